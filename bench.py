@@ -1,0 +1,348 @@
+"""Benchmark of the rebin path: views/s at 3M Gaussians, SH degree 3, 1080p.
+
+Workload (the headline configuration): a 3,000,000-splat scene of 64
+isotropic clusters with SH degree 3 colour, rendered at 1920x1080 with 16x16
+tiles from a 64-pose orbit (radius 12, +-20 degree elevation jitter).  One
+step = one pass of the rebin path over every view of the orbit.  The scene is
+uploaded once (as SceneSyncer does); inputs (732 MB of splat data) are larger
+than the 129 MB L2, so no L2 flush is interposed.
+
+Arms:
+  default             the library through its C ABI, CUDA events on the stream
+                      the library enqueues on; `e2e` re-times the same views
+                      through the public C entry point with host camera
+                      structs in and a device->pinned-host image copy out.
+  --impl reference    the reference path's CPU restatement (the oracle, all
+                      host threads) on a bounded sample: one view per step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "webgpu-3dgs_gb300"))
+
+METRIC = "views/s at 3M Gaussians 1080p, learned+batched vs plain, same image"
+WORKLOAD = ("3M Gaussians fp32 SH3 (64 clusters, seed 0), 1920x1080, 16x16 tiles, "
+            "64-pose orbit r=12 +-20deg")
+N_SPLATS, WIDTH, HEIGHT, TILE = 3_000_000, 1920, 1080, 16
+STAGES = ["preprocess-splats", "prefix-scan", "emit-tile-refs", "radix-sort",
+          "identify-tile-ranges", "rasterize-tiles"]
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(n_views: int):
+    from gs3d import scenes
+    data = scenes.scene_clusters(N_SPLATS, seed=0, sh_degree=3)
+    eyes = scenes.orbit_eyes(64, radius=12.0, jitter_deg=20.0, seed=0)
+    cams = [scenes.camera_at(eyes[i % 64], WIDTH, HEIGHT).getUniformData(WIDTH, HEIGHT)
+            for i in range(n_views)]
+    return data, cams
+
+
+def algorithmic_bytes(n, R, tiles, passes, sh_floats):
+    """Bytes each stage must move at minimum (per view)."""
+    return {
+        "preprocess-splats": n * (64 + 4 * sh_floats) + n * (64 + 4),
+        "prefix-scan": 8 * n,
+        "emit-tile-refs": n * (24 + 4) + 12 * R,
+        "radix-sort": 8 * R + passes * 24 * R,
+        "identify-tile-ranges": 4 * R + 4 * (tiles + 1),
+        "rasterize-tiles": 44 * R + 8 * WIDTH * HEIGHT,
+    }
+
+
+def run_ours(args, rank, world):
+    import torch
+
+    from gs3d import _lib
+    from gs3d.camera import camera_struct
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()
+    lib = _lib.load()
+    ctx = C.c_void_p()
+    cfg = _lib.Config_t(dev, TILE, TILE, 16, C.c_void_p(stream.cuda_stream), 0)
+    rc = lib.gs3d_create(C.byref(ctx), C.byref(cfg))
+    if rc != 0:
+        raise RuntimeError(f"gs3d_create failed: {rc}")
+
+    def check(rc):
+        if rc != 0:
+            raise RuntimeError(lib.gs3d_last_error(ctx).decode())
+
+    data, cams = make_workload(args.views)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    check(lib.gs3d_set_splats(ctx, data.splatCount, ptr(data.positions), ptr(data.scales),
+                              ptr(data.rotations), ptr(data.colors),
+                              ptr(data.sphericalHarmonics), 3, 0))
+    cam_structs = [camera_struct(u) for u in cams]
+    stage_fns = [lib.gs3d_preprocess, lib.gs3d_prefix_scan, lib.gs3d_emit_tile_refs,
+                 lib.gs3d_radix_sort, lib.gs3d_identify_tile_ranges, lib.gs3d_rasterize_tiles]
+
+    # first pass: size the key buffers (grow on overflow) and record ref counts
+    refs = []
+    for cs in cam_structs:
+        for _ in range(3):
+            check(lib.gs3d_rebin(ctx, C.byref(cs), WIDTH, HEIGHT))
+            rc = lib.gs3d_synchronize(ctx)
+            if rc != _lib.ERR_CAPACITY:
+                check(rc)
+                break
+        r = C.c_uint32()
+        check(lib.gs3d_ref_count(ctx, C.byref(r)))
+        refs.append(r.value)
+
+    def one_step(events=None):
+        for v, cs in enumerate(cam_structs):
+            check(lib.gs3d_set_camera(ctx, C.byref(cs), WIDTH, HEIGHT))
+            for s, fn in enumerate(stage_fns):
+                if events is not None:
+                    events[v][s].record(stream)
+                check(fn(ctx))
+            if events is not None:
+                events[v][len(stage_fns)].record(stream)
+
+    for _ in range(args.warmup):
+        one_step()
+    check(lib.gs3d_synchronize(ctx))
+
+    ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(len(stage_fns) + 1)]
+           for _ in cam_structs] for _ in range(args.steps)]
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clocks:
+        start.record(stream)
+        for k in range(args.steps):
+            one_step(ev[k])
+        stop.record(stream)
+        torch.cuda.synchronize()
+    check(lib.gs3d_synchronize(ctx))
+    total_ms = start.elapsed_time(stop)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    stage_ms = np.zeros(len(stage_fns))
+    for k in range(args.steps):
+        for v in range(len(cam_structs)):
+            for s in range(len(stage_fns)):
+                stage_ms[s] += ev[k][v][s].elapsed_time(ev[k][v][s + 1])
+    views = args.steps * len(cam_structs)
+    stage_ms /= views  # per view
+
+    # ---- e2e: public entry point, host camera in, pinned host image out ----
+    img_bytes = WIDTH * HEIGHT * 8
+    pinned = torch.empty(img_bytes * 2, dtype=torch.uint8, pin_memory=True)
+    e2e_views = min(len(cam_structs), 32)
+    for _ in range(2):
+        check(lib.gs3d_rebin(ctx, C.byref(cam_structs[0]), WIDTH, HEIGHT))
+    check(lib.gs3d_synchronize(ctx))
+    t0 = time.perf_counter()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        for v in range(e2e_views):
+            cs = camera_struct(cams[v])  # host struct built per view
+            check(lib.gs3d_rebin(ctx, C.byref(cs), WIDTH, HEIGHT))
+            check(lib.gs3d_copy_buffer_async(ctx, 14, C.c_void_p(pinned.data_ptr() +
+                                                                  (v % 2) * img_bytes), img_bytes))
+    e1.record(stream)
+    check(lib.gs3d_synchronize(ctx))
+    e2e_wall = time.perf_counter() - t0
+    e2e_ms = e0.elapsed_time(e1)
+    e2e_views_total = args.steps * e2e_views
+
+    lib.gs3d_destroy(ctx)
+
+    # ---- roofline of the dominant HBM-bound kernel ----
+    tiles = (WIDTH // TILE) * -(-HEIGHT // TILE)
+    tile_bits = (tiles - 1).bit_length()
+    plan_passes = 4 + (tile_bits + 7) // 8  # depth digits + non-zero tile-id digits
+    mean_R = float(np.mean(refs))
+    algo = algorithmic_bytes(N_SPLATS, mean_R, tiles, plan_passes, 45)
+    peak, peak_kind = peaks()
+    per_stage = {}
+    for s, name in enumerate(STAGES):
+        gbs = algo[name] / (stage_ms[s] * 1e-3) / 1e9
+        per_stage[name] = {"ms": round(float(stage_ms[s]), 4), "algo_bytes": int(algo[name]),
+                           "gbs": round(gbs, 1), "frac_hbm": round(gbs / peak, 3)}
+    hbm_stages = [s for s in STAGES if s != "rasterize-tiles"]
+    dom = max(hbm_stages, key=lambda s: per_stage[s]["ms"])
+    value = views * world / (total_ms * 1e-3)  # weak scaling: every rank renders its views
+    return {
+        "value": value, "ms_per_step": total_ms / args.steps, "views": views,
+        "per_stage": per_stage, "dominant": dom, "peak": peak, "peak_kind": peak_kind,
+        "mean_refs": mean_R, "passes": plan_passes, "clocks": clocks.summary(),
+        "e2e_value": e2e_views_total * world / (e2e_ms * 1e-3),
+        "e2e_wall_value": e2e_views_total / e2e_wall,
+        "h2d": 288 * len(cam_structs), "d2h": img_bytes * len(cam_structs),
+        "launches_per_view": 5 + plan_passes + 1,
+    }
+
+
+def cpu_view_seconds(n_views=1, threads=0):
+    """Times the oracle's whole rebin on one full-size view (bounded sample)."""
+    from oracle import Oracle
+    o = Oracle()
+    data, cams = make_workload(n_views)
+    t = o.max_threads() if threads == 0 else threads
+    times = []
+    for u in cams:
+        t0 = time.perf_counter()
+        o.rebin(u, WIDTH, HEIGHT, TILE, TILE, data.positions, data.scales, data.rotations,
+                data.colors, data.sphericalHarmonics, 3, threads=t,
+                key_capacity=N_SPLATS * 16)
+        times.append(time.perf_counter() - t0)
+    return times, t
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--views", type=int, default=64)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        times, threads = cpu_view_seconds(args.warmup + args.steps)
+        timed = times[args.warmup:]
+        v = len(timed) / sum(timed)
+        sample = f"one full 3M-splat SH3 1080p view per step ({len(timed)} views of the orbit)"
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": v, "unit": "views/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(timed) / len(timed), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "views_per_step": 1, "threads": threads},
+            "cpu_baseline": {"value": v, "unit": "views/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "views/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+        }))
+        return
+
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    res = run_ours(args, rank, world)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        times, threads = cpu_view_seconds(1)
+        cpu = {"value": 1.0 / times[0], "unit": "views/s", "cores": threads, "kind": "port",
+               "sample": "one full 3M-splat SH3 1080p view (orbit pose 0), oracle rebin"}
+    if rank == 0:
+        dom = res["per_stage"][res["dominant"]]
+        out = {
+            "metric": METRIC, "value": res["value"], "unit": "views/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "path": "plain single-view",
+                       "views_per_step": args.views, "l2": "inputs larger than L2 (no flush)",
+                       "mean_refs_per_view": res["mean_refs"], "sort_passes": res["passes"]},
+            "roofline": {"bound": "hbm", "kernel": res["dominant"], "achieved": dom["gbs"],
+                         "peak": res["peak"], "unit": "GB/s", "frac": dom["frac_hbm"],
+                         "peak_kind": res["peak_kind"], "traffic": None},
+            "stages": res["per_stage"],
+            "cpu_baseline": cpu,
+            "e2e": {"value": res["e2e_value"], "unit": "views/s",
+                    "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
+                    "wall_value": res["e2e_wall_value"]},
+            "gpu_launches": res["launches_per_view"] * res["views"],
+            "clocks": res["clocks"],
+        }
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

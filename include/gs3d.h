@@ -1,0 +1,185 @@
+/*
+ * gs3d.h - C ABI of the GB300 (sm_103a) Gaussian-splat rebin library.
+ *
+ * The library replaces the per-frame rebin path of the webgpu-3dgs renderer
+ * (src/renderers/GaussianSplatRenderer.ts:1104-1266):
+ *
+ *   preprocess -> exclusive prefix scan -> (tile|depth) key emit
+ *   -> 64-bit LSD radix sort -> tile-range identify -> tiled alpha-blend raster
+ *
+ * Every entry point takes plain pointers and sizes and returns an int status
+ * (GS3D_OK = 0).  Work is stream ordered and asynchronous: a call returns once
+ * its kernels are enqueued.  Device-side failures (key capacity overflow, a
+ * bounded spin that ran out) are latched in a device word and reported by the
+ * next gs3d_synchronize() or copy-out.  A context is single-threaded, like the
+ * JavaScript thread that drives the reference renderer; separate contexts may
+ * be driven from separate threads.
+ *
+ * Buffer layouts are the reference's: the four splat arrays of SceneSyncer
+ * (vec4 f32 each), the 64-byte ProjectedSplat, interleaved u32 [hi, lo] sort
+ * keys, u32 sort values, u32 tile_offsets[T+1] and an rgba16float image.
+ */
+#ifndef GS3D_H
+#define GS3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GS3D_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+#define GS3D_OK                0
+#define GS3D_ERR_INVALID_ARG   1  /* null pointer, bad size, bad enum        */
+#define GS3D_ERR_OOM           2  /* cudaMalloc / pinned allocation failed   */
+#define GS3D_ERR_CAPACITY      3  /* live ref count exceeded the key buffers;
+                                     capacity has been grown, re-run rebin   */
+#define GS3D_ERR_CUDA          4  /* any other CUDA runtime error            */
+#define GS3D_ERR_TIMEOUT       5  /* a bounded device spin gave up           */
+#define GS3D_ERR_STATE         6  /* call order: e.g. raster before rebin    */
+#define GS3D_ERR_NO_DEVICE     7  /* no CUDA device / wrong architecture     */
+
+/* ---- plain-old-data types mirrored from the reference ------------------ */
+
+/* CameraUniforms (src/shaders/compute/preprocess_splats.wgsl:1-8), filled by
+ * Camera.getUniformData (src/Camera.ts:172-191): column-major f32 mat4s. */
+typedef struct gs3d_camera {
+    float view[16];
+    float projection[16];
+    float inverse_view[16];
+    float inverse_projection[16];
+    float position[4];   /* x, y, z, 1                       */
+    float viewport[4];   /* width, height, width/height, 0   */
+} gs3d_camera;
+
+/* ProjectedSplat (preprocess_splats.wgsl:18-31), stride 64 bytes
+ * (src/types/config.ts:2). */
+typedef struct gs3d_projected_splat {
+    float mean_px[2];
+    float depth;         /* view-space z (negative in front)  */
+    float radius_px;
+    float conic[3];
+    float opacity;
+    float color[3];
+    uint32_t valid;
+    uint32_t tile_min[2];
+    uint32_t tile_max[2];
+} gs3d_projected_splat;
+
+typedef struct gs3d_config {
+    int      device;              /* CUDA ordinal                                  */
+    uint32_t tile_w, tile_h;      /* tile pixel size; 0 -> 16x16 (Scene.ts:6)      */
+    uint32_t max_tiles_per_splat; /* initial key capacity = N * this; 0 -> 16
+                                     (config.ts:4).  Grown on overflow, never
+                                     truncated.                                    */
+    void*    stream;              /* cudaStream_t to enqueue on; NULL -> the
+                                     library creates a non-blocking stream         */
+    uint32_t flags;               /* reserved, 0                                   */
+} gs3d_config;
+
+/* Named device buffers (BufferManager names, GaussianSplatRenderer.ts:338-465). */
+typedef enum gs3d_buffer {
+    GS3D_BUF_SPLAT_POSITIONS   = 0,  /* vec4 f32 x N                               */
+    GS3D_BUF_SPLAT_SCALES      = 1,
+    GS3D_BUF_SPLAT_ROTATIONS   = 2,  /* (w, x, y, z)                               */
+    GS3D_BUF_SPLAT_COLORS      = 3,  /* rgba                                       */
+    GS3D_BUF_SPLAT_SH_REST     = 4,  /* f32 x N x 3*((deg+1)^2-1), f_rest order    */
+    GS3D_BUF_PROJECTED_SPLATS  = 5,  /* gs3d_projected_splat x N                   */
+    GS3D_BUF_SPLAT_REF_COUNTS  = 6,  /* u32 x N                                    */
+    GS3D_BUF_SPLAT_REF_OFFSETS = 7,  /* u32 x (N+1), [N] = total                   */
+    GS3D_BUF_REF_COUNTER       = 8,  /* u32 x 1 (live ref count R)                 */
+    GS3D_BUF_SORT_KEYS_A       = 9,  /* u32 [hi=tile, lo=bits(-depth)] x capacity;
+                                        holds the sorted keys after a rebin        */
+    GS3D_BUF_SORT_VALUES_A     = 10, /* u32 splat id x capacity (sorted)           */
+    GS3D_BUF_SORT_KEYS_B       = 11, /* ping-pong partner                          */
+    GS3D_BUF_SORT_VALUES_B     = 12,
+    GS3D_BUF_TILE_OFFSETS      = 13, /* u32 x (T+1)                                */
+    GS3D_BUF_SPLAT_TARGET      = 14, /* rgba16float x W x H (premultiplied)        */
+    GS3D_BUF_TILE_COSTS        = 15, /* u32 x T: splats iterated before the tile's
+                                        last pixel terminated (extension)          */
+    GS3D_BUF_COUNT_            = 16
+} gs3d_buffer;
+
+/* ---- lifetime ----------------------------------------------------------- */
+
+/* GaussianSplatRenderer constructor + init (GaussianSplatRenderer.ts:331-471). */
+int gs3d_create(struct gs3d_ctx** out_ctx, const gs3d_config* cfg);
+int gs3d_destroy(struct gs3d_ctx* ctx);
+/* Human-readable text of the last failing call on this context (never NULL). */
+const char* gs3d_last_error(const struct gs3d_ctx* ctx);
+int gs3d_abi_version(void);
+
+/* ---- scene ---------------------------------------------------------------- */
+
+/* SceneSyncer.setSplatData (src/SceneSyncer.ts:25-38): copies the splat SoA
+ * (vec4 f32 per splat) into library-owned device buffers.  sh_rest may be NULL
+ * (degree 0, the reference's only colour path); otherwise it holds
+ * 3*((sh_degree+1)^2-1) floats per splat in PLY f_rest order
+ * (src/workers/SceneWorker.ts:457-463).  memory: 0 = host pointers,
+ * 1 = device pointers.  Binning buffers are resized as in
+ * GaussianSplatRenderer.resizeBinningBuffers (:209-227). */
+int gs3d_set_splats(struct gs3d_ctx* ctx, uint32_t n,
+                    const float* positions, const float* scales,
+                    const float* rotations, const float* colors,
+                    const float* sh_rest, uint32_t sh_degree, int memory);
+
+/* setTileSize (GaussianSplatRenderer.ts:301-317): clamps to the device limit
+ * (tile_w * tile_h <= 1024) and reports the size in use. */
+int gs3d_set_tile_size(struct gs3d_ctx* ctx, uint32_t tile_w, uint32_t tile_h,
+                       uint32_t* out_tile_w, uint32_t* out_tile_h);
+
+/* The uniform writes at the top of rebin (GaussianSplatRenderer.ts:1112-1131)
+ * plus Viewport's camera upload (src/Viewport.ts:183): sets the camera and the
+ * viewport; resizes tile_offsets and the splat target on a viewport change
+ * (resizeViewportTargets, :231-295). */
+int gs3d_set_camera(struct gs3d_ctx* ctx, const gs3d_camera* cam,
+                    uint32_t width, uint32_t height);
+
+/* ---- stages (rebin, GaussianSplatRenderer.ts:1143-1265) ------------------- */
+int gs3d_preprocess(struct gs3d_ctx* ctx);          /* preprocess_splats.wgsl      */
+int gs3d_prefix_scan(struct gs3d_ctx* ctx);         /* prefix_scan_{local,blocks,add} */
+int gs3d_emit_tile_refs(struct gs3d_ctx* ctx);      /* emit_tile_refs.wgsl         */
+int gs3d_radix_sort(struct gs3d_ctx* ctx);          /* radix_{histogram,scatter}, scan_{local,add} */
+int gs3d_identify_tile_ranges(struct gs3d_ctx* ctx);/* identify_tile_ranges.wgsl   */
+int gs3d_rasterize_tiles(struct gs3d_ctx* ctx);     /* rasterize_tiles.wgsl        */
+
+/* rebin (GaussianSplatRenderer.ts:1104-1266): set_camera + all six stages. */
+int gs3d_rebin(struct gs3d_ctx* ctx, const gs3d_camera* cam,
+               uint32_t width, uint32_t height);
+
+/* Waits for the context's stream and reports latched device errors.  After
+ * GS3D_ERR_CAPACITY the key buffers have already been grown to the observed
+ * ref count; re-issue the rebin. */
+int gs3d_synchronize(struct gs3d_ctx* ctx);
+
+/* ---- buffer access ---------------------------------------------------------- */
+
+/* Device pointer and size in bytes of a named buffer (for zero-copy callers). */
+int gs3d_buffer_info(struct gs3d_ctx* ctx, gs3d_buffer which,
+                     void** device_ptr, size_t* bytes);
+/* Blocking copy-out of the first `bytes` bytes of a named buffer. */
+int gs3d_read_buffer(struct gs3d_ctx* ctx, gs3d_buffer which,
+                     void* host_dst, size_t bytes);
+/* Blocking copy-in (stage-wise parity: feed another implementation's
+ * intermediate buffer into the next stage). */
+int gs3d_write_buffer(struct gs3d_ctx* ctx, gs3d_buffer which,
+                      const void* host_src, size_t bytes);
+/* Stream-ordered copy-out of the first `bytes` bytes of a named buffer into
+ * host memory (asynchronous when host_dst is page-locked).  The copy lands
+ * once gs3d_synchronize returns.  Replaces the reference's staging-buffer
+ * readback (mapAsync, GaussianSplatRenderer.ts:1287-1295). */
+int gs3d_copy_buffer_async(struct gs3d_ctx* ctx, gs3d_buffer which,
+                           void* host_dst, size_t bytes);
+/* Live ref count of the last rebin (blocking read of ref_counter). */
+int gs3d_ref_count(struct gs3d_ctx* ctx, uint32_t* out_count);
+/* readTileCounts (GaussianSplatRenderer.ts:1278-1310): per-tile key counts
+ * max(0, off[t+1]-off[t]); `n` must be >= tile count. */
+int gs3d_read_tile_counts(struct gs3d_ctx* ctx, uint32_t* counts, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GS3D_H */

@@ -1,0 +1,581 @@
+// ctx.cu - context, buffer ownership and the C ABI of include/gs3d.h.
+//
+// Mirrors the host side of the reference renderer:
+//   - gs3d_create / gs3d_destroy: GaussianSplatRenderer constructor + init
+//     (src/renderers/GaussianSplatRenderer.ts:331-471) and the BufferManager
+//     buffers it creates (:338-465);
+//   - gs3d_set_splats: SceneSyncer.setSplatData (src/SceneSyncer.ts:25-38)
+//     followed by resizeBinningBuffers (:209-227);
+//   - gs3d_set_camera: the uniform uploads of rebin (:1112-1131) and, on a
+//     viewport change, resizeViewportTargets (:231-295);
+//   - gs3d_rebin: the stage sequence of rebin (:1104-1266).
+//
+// Differences by design: no dispatch or buffer clamping (the reference clamps
+// dispatch counts to maxComputeWorkgroupsPerDimension and buffers to
+// maxStorageBufferBindingSize, silently truncating large scenes); the key
+// buffers start at N * max_tiles_per_splat entries like the reference but
+// overflow is detected on the device and reported, after which the buffers
+// are grown and the caller re-issues the rebin.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "gs3d_internal.cuh"
+
+using namespace gs3d;
+
+namespace {
+
+// Look-back status words carry 30-bit values, which bounds the live count.
+constexpr uint32_t kMaxCapacity = (1u << 30) - 1u;
+constexpr int kFrameSlots = 8;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+__global__ void probe_kernel(int* out) {
+  if (out) *out = 1;
+}
+
+}  // namespace
+
+struct gs3d_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int sm_count = 0;
+  std::string err = "no error";
+
+  uint32_t tile_w = 16, tile_h = 16, max_tiles_per_splat = 16;
+
+  // scene (SceneSyncer buffers)
+  bool have_scene = false;
+  uint32_t n = 0, sh_degree = 0;
+  DevBuf pos, scale, rot, color, sh;
+
+  // binning (GaussianSplatRenderer buffers)
+  DevBuf proj, counts, offsets, ref_counter;
+  DevBuf keys_a, vals_a, keys_b, vals_b;
+  uint32_t capacity = 0;
+  DevBuf scan_status, sort_status;
+  uint32_t scan_epoch = 0;
+
+  // frame
+  bool have_camera = false;
+  DevBuf frame;
+  FrameUniforms* h_frames = nullptr;  // pinned ring
+  cudaEvent_t frame_ev[kFrameSlots] = {};
+  int frame_slot = 0;
+  uint32_t W = 0, H = 0, tiles_x = 0, tiles_y = 0;
+  DevBuf tile_offsets, image, tile_costs;
+
+  DevBuf ctrl;
+  uint32_t* h_word = nullptr;  // pinned scratch for small reads
+};
+
+namespace {
+
+int fail(gs3d_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+int cuda_fail(gs3d_ctx* c, cudaError_t e, const char* what) {
+  const int code = (e == cudaErrorMemoryAllocation) ? GS3D_ERR_OOM
+                   : (e == cudaErrorNoKernelImageForDevice || e == cudaErrorNoDevice ||
+                      e == cudaErrorInsufficientDriver)
+                       ? GS3D_ERR_NO_DEVICE
+                       : GS3D_ERR_CUDA;
+  return fail(c, code, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                   \
+  do {                                                   \
+    cudaError_t e_ = (expr);                             \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+  } while (0)
+
+void release(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+// Grow-only allocation; contents are not preserved.
+int ensure(gs3d_ctx* c, DevBuf& b, size_t bytes, const char* name) {
+  if (bytes == 0) bytes = 16;
+  if (b.bytes >= bytes) return GS3D_OK;
+  if (b.p) {
+    CK(cudaStreamSynchronize(c->stream), "synchronize before resize");
+    release(b);
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, GS3D_ERR_OOM, "cudaMalloc of %zu bytes for %s failed: %s", bytes, name,
+                cudaGetErrorString(e));
+  }
+  b.p = p;
+  b.bytes = bytes;
+  return GS3D_OK;
+}
+
+#define TRY(expr)                 \
+  do {                            \
+    const int r_ = (expr);        \
+    if (r_ != GS3D_OK) return r_; \
+  } while (0)
+
+int ensure_key_capacity(gs3d_ctx* c, uint64_t want) {
+  if (want > kMaxCapacity)
+    return fail(c, GS3D_ERR_CAPACITY, "%llu tile refs exceed the %u-ref limit of one rebin",
+                (unsigned long long)want, kMaxCapacity);
+  if (want <= c->capacity && c->keys_a.p) return GS3D_OK;
+  const uint32_t cap = (uint32_t)std::max<uint64_t>(want, 1);
+  TRY(ensure(c, c->keys_a, (size_t)cap * sizeof(uint2), "sort_keys_a"));
+  TRY(ensure(c, c->keys_b, (size_t)cap * sizeof(uint2), "sort_keys_b"));
+  TRY(ensure(c, c->vals_a, (size_t)cap * sizeof(uint32_t), "sort_values_a"));
+  TRY(ensure(c, c->vals_b, (size_t)cap * sizeof(uint32_t), "sort_values_b"));
+  TRY(ensure(c, c->sort_status, sort_status_words(cap, kMaxSortPasses) * sizeof(uint32_t),
+             "sort look-back status"));
+  c->capacity = cap;
+  return GS3D_OK;
+}
+
+int set_device(gs3d_ctx* c) {
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
+  return GS3D_OK;
+}
+
+Ctrl* ctrl_of(gs3d_ctx* c) { return static_cast<Ctrl*>(c->ctrl.p); }
+
+int require_frame(gs3d_ctx* c, const char* stage) {
+  if (!c->have_scene) return fail(c, GS3D_ERR_STATE, "%s: no splats set", stage);
+  if (!c->have_camera) return fail(c, GS3D_ERR_STATE, "%s: no camera set", stage);
+  return GS3D_OK;
+}
+
+// Reads the latched device error word (stream must be idle) and clears it.
+int check_device_errors(gs3d_ctx* c) {
+  CK(cudaMemcpy(c->h_word, &ctrl_of(c)->error, sizeof(uint32_t), cudaMemcpyDeviceToHost),
+     "read error word");
+  const uint32_t e = c->h_word[0];
+  if (e == 0) return GS3D_OK;
+  CK(cudaMemset(&ctrl_of(c)->error, 0, sizeof(uint32_t)), "clear error word");
+  if (e & DEVERR_CAPACITY) {
+    CK(cudaMemcpy(c->h_word, c->ref_counter.p, sizeof(uint32_t), cudaMemcpyDeviceToHost),
+       "read ref_counter");
+    const uint64_t r = c->h_word[0];
+    if (r > kMaxCapacity)
+      return fail(c, GS3D_ERR_CAPACITY, "%llu tile refs exceed the %u-ref limit of one rebin",
+                  (unsigned long long)r, kMaxCapacity);
+    TRY(ensure_key_capacity(c, std::min<uint64_t>(r + r / 8 + 1024, kMaxCapacity)));
+    return fail(c, GS3D_ERR_CAPACITY,
+                "live ref count %llu exceeded the key capacity; capacity is now %u, re-run "
+                "the rebin",
+                (unsigned long long)r, c->capacity);
+  }
+  if (e & DEVERR_TIMEOUT)
+    return fail(c, GS3D_ERR_TIMEOUT, "a bounded device wait gave up (look-back or bulk copy)");
+  return fail(c, GS3D_ERR_INVALID_ARG,
+              "a sort key's tile id or a splat offset was out of range for this frame");
+}
+
+int sync_and_check(gs3d_ctx* c) {
+  CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return check_device_errors(c);
+}
+
+}  // namespace
+
+extern "C" {
+
+int gs3d_abi_version(void) { return GS3D_ABI_VERSION; }
+
+const char* gs3d_last_error(const gs3d_ctx* c) {
+  return c ? c->err.c_str() : "null context";
+}
+
+int gs3d_create(gs3d_ctx** out, const gs3d_config* cfg) {
+  if (!out) return GS3D_ERR_INVALID_ARG;
+  *out = nullptr;
+  gs3d_ctx* c = new (std::nothrow) gs3d_ctx();
+  if (!c) return GS3D_ERR_OOM;
+  gs3d_config def{};
+  if (!cfg) cfg = &def;
+  c->device = cfg->device;
+  if (cfg->tile_w) c->tile_w = cfg->tile_w;
+  if (cfg->tile_h) c->tile_h = cfg->tile_h;
+  if (cfg->max_tiles_per_splat) c->max_tiles_per_splat = cfg->max_tiles_per_splat;
+  auto bail = [&](int rc) {
+    gs3d_destroy(c);
+    return rc;
+  };
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count <= c->device || c->device < 0) {
+    cudaGetLastError();
+    return bail(GS3D_ERR_NO_DEVICE);
+  }
+  if (set_device(c) != GS3D_OK) return bail(GS3D_ERR_NO_DEVICE);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess) return bail(GS3D_ERR_NO_DEVICE);
+  if (prop.major != 10 || prop.minor != 3) {
+    fprintf(stderr, "gs3d: device %d is sm_%d%d; this library is built for sm_103a only\n",
+            c->device, prop.major, prop.minor);
+    return bail(GS3D_ERR_NO_DEVICE);
+  }
+  c->sm_count = prop.multiProcessorCount;
+  if (cfg->stream) {
+    c->stream = static_cast<cudaStream_t>(cfg->stream);
+  } else {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+      return bail(GS3D_ERR_CUDA);
+    c->own_stream = true;
+  }
+  probe_kernel<<<1, 1, 0, c->stream>>>(nullptr);
+  if (cudaGetLastError() != cudaSuccess) return bail(GS3D_ERR_NO_DEVICE);
+  if (ensure(c, c->frame, sizeof(FrameUniforms), "frame uniforms") != GS3D_OK ||
+      ensure(c, c->ctrl, sizeof(Ctrl), "control block") != GS3D_OK ||
+      ensure(c, c->ref_counter, 16, "ref_counter") != GS3D_OK)
+    return bail(GS3D_ERR_OOM);
+  if (cudaMallocHost(&c->h_frames, sizeof(FrameUniforms) * kFrameSlots) != cudaSuccess ||
+      cudaMallocHost(&c->h_word, 64) != cudaSuccess)
+    return bail(GS3D_ERR_OOM);
+  for (int i = 0; i < kFrameSlots; ++i)
+    if (cudaEventCreateWithFlags(&c->frame_ev[i], cudaEventDisableTiming) != cudaSuccess)
+      return bail(GS3D_ERR_CUDA);
+  if (cudaMemsetAsync(c->ctrl.p, 0, sizeof(Ctrl), c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->ref_counter.p, 0, 16, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return bail(GS3D_ERR_CUDA);
+  *out = c;
+  return GS3D_OK;
+}
+
+int gs3d_destroy(gs3d_ctx* c) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  DevBuf* bufs[] = {&c->pos,        &c->scale,        &c->rot,         &c->color,
+                    &c->sh,         &c->proj,         &c->counts,      &c->offsets,
+                    &c->ref_counter, &c->keys_a,      &c->vals_a,      &c->keys_b,
+                    &c->vals_b,     &c->scan_status,  &c->sort_status, &c->frame,
+                    &c->tile_offsets, &c->image,      &c->tile_costs,  &c->ctrl};
+  for (DevBuf* b : bufs) release(*b);
+  for (int i = 0; i < kFrameSlots; ++i)
+    if (c->frame_ev[i]) cudaEventDestroy(c->frame_ev[i]);
+  if (c->h_frames) cudaFreeHost(c->h_frames);
+  if (c->h_word) cudaFreeHost(c->h_word);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return GS3D_OK;
+}
+
+int gs3d_set_splats(gs3d_ctx* c, uint32_t n, const float* positions, const float* scales,
+                    const float* rotations, const float* colors, const float* sh_rest,
+                    uint32_t sh_degree, int memory) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  if (memory != 0 && memory != 1) return fail(c, GS3D_ERR_INVALID_ARG, "memory must be 0 or 1");
+  if (sh_degree > 3) return fail(c, GS3D_ERR_INVALID_ARG, "sh_degree %u > 3", sh_degree);
+  if (n > 0 && (!positions || !scales || !rotations || !colors))
+    return fail(c, GS3D_ERR_INVALID_ARG, "null splat array");
+  if (n > 0 && sh_degree > 0 && !sh_rest)
+    return fail(c, GS3D_ERR_INVALID_ARG, "sh_degree %u needs sh_rest", sh_degree);
+  if (n > (1u << 30)) return fail(c, GS3D_ERR_INVALID_ARG, "too many splats (%u)", n);
+  TRY(set_device(c));
+  const size_t v4 = (size_t)n * 16;
+  const uint32_t kc = 3u * ((sh_degree + 1) * (sh_degree + 1) - 1);
+  TRY(ensure(c, c->pos, v4, "splat_positions"));
+  TRY(ensure(c, c->scale, v4, "splat_scales"));
+  TRY(ensure(c, c->rot, v4, "splat_rotations"));
+  TRY(ensure(c, c->color, v4, "splat_colors"));
+  if (kc) TRY(ensure(c, c->sh, (size_t)n * kc * sizeof(float), "splat_sh_rest"));
+  const cudaMemcpyKind kind = memory ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (n) {
+    CK(cudaMemcpyAsync(c->pos.p, positions, v4, kind, c->stream), "upload positions");
+    CK(cudaMemcpyAsync(c->scale.p, scales, v4, kind, c->stream), "upload scales");
+    CK(cudaMemcpyAsync(c->rot.p, rotations, v4, kind, c->stream), "upload rotations");
+    CK(cudaMemcpyAsync(c->color.p, colors, v4, kind, c->stream), "upload colors");
+    if (kc)
+      CK(cudaMemcpyAsync(c->sh.p, sh_rest, (size_t)n * kc * sizeof(float), kind, c->stream),
+         "upload sh_rest");
+  }
+  // resizeBinningBuffers (GaussianSplatRenderer.ts:209-227)
+  TRY(ensure(c, c->proj, (size_t)n * sizeof(gs3d_projected_splat), "projected_splats"));
+  TRY(ensure(c, c->counts, (size_t)n * 4, "splat_ref_counts"));
+  TRY(ensure(c, c->offsets, ((size_t)n + 1) * 4, "splat_ref_offsets"));
+  TRY(ensure(c, c->scan_status, scan_status_words(n) * 8, "scan look-back status"));
+  TRY(ensure_key_capacity(
+      c, std::min<uint64_t>((uint64_t)std::max<uint32_t>(n, 1) * c->max_tiles_per_splat,
+                            kMaxCapacity)));
+  CK(cudaStreamSynchronize(c->stream), "splat upload");
+  c->n = n;
+  c->sh_degree = sh_degree;
+  c->have_scene = true;
+  return GS3D_OK;
+}
+
+int gs3d_set_tile_size(gs3d_ctx* c, uint32_t tx, uint32_t ty, uint32_t* out_x, uint32_t* out_y) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  // clampTileSize (GaussianSplatRenderer.ts:162-167) with CUDA's 1024-thread block limit
+  tx = std::max<uint32_t>(1, std::min<uint32_t>(tx ? tx : 1, 1024));
+  ty = std::max<uint32_t>(1, std::min<uint32_t>(ty ? ty : 1, 1024 / tx));
+  if (tx != c->tile_w || ty != c->tile_h) {
+    c->tile_w = tx;
+    c->tile_h = ty;
+    c->have_camera = false;  // tile grid recomputed at the next set_camera
+  }
+  if (out_x) *out_x = tx;
+  if (out_y) *out_y = ty;
+  return GS3D_OK;
+}
+
+int gs3d_set_camera(gs3d_ctx* c, const gs3d_camera* cam, uint32_t width, uint32_t height) {
+  if (!c || !cam) return fail(c, GS3D_ERR_INVALID_ARG, "null camera");
+  TRY(set_device(c));
+  width = std::max<uint32_t>(1, width);  // GaussianSplatRenderer.ts:1040-1041
+  height = std::max<uint32_t>(1, height);
+  const uint32_t tx = (width + c->tile_w - 1) / c->tile_w;  // :1042-1043
+  const uint32_t ty = (height + c->tile_h - 1) / c->tile_h;
+  const uint64_t tiles = (uint64_t)tx * ty;
+  if (tiles >= (1ull << 31)) return fail(c, GS3D_ERR_INVALID_ARG, "viewport too large");
+  TRY(ensure(c, c->tile_offsets, (tiles + 1) * 4, "tile_offsets"));
+  TRY(ensure(c, c->tile_costs, tiles * 4, "tile_costs"));
+  TRY(ensure(c, c->image, (size_t)width * height * 8, "splat_target"));
+  c->W = width;
+  c->H = height;
+  c->tiles_x = tx;
+  c->tiles_y = ty;
+
+  const int slot = c->frame_slot;
+  c->frame_slot = (slot + 1) % kFrameSlots;
+  CK(cudaEventSynchronize(c->frame_ev[slot]), "frame slot reuse");
+  FrameUniforms& f = c->h_frames[slot];
+  std::memset(&f, 0, sizeof(f));
+  f.cam = *cam;
+  f.tile_count[0] = tx;
+  f.tile_count[1] = ty;
+  f.splat_count = c->n;
+  f.num_tiles = (uint32_t)tiles;
+  f.inv_tile[0] = (float)(1.0 / c->tile_w);  // :1127-1128, f64 division stored as f32
+  f.inv_tile[1] = (float)(1.0 / c->tile_h);
+  f.viewport[0] = width;
+  f.viewport[1] = height;
+  f.tile_size[0] = c->tile_w;
+  f.tile_size[1] = c->tile_h;
+  CK(cudaMemcpyAsync(c->frame.p, &f, sizeof(f), cudaMemcpyHostToDevice, c->stream),
+     "upload frame uniforms");
+  CK(cudaEventRecord(c->frame_ev[slot], c->stream), "frame event");
+  c->have_camera = true;
+  return GS3D_OK;
+}
+
+int gs3d_preprocess(gs3d_ctx* c) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  TRY(require_frame(c, "preprocess"));
+  TRY(set_device(c));
+  // start of a frame: counters, histograms and the error latch
+  CK(cudaMemsetAsync(c->ctrl.p, 0, sizeof(Ctrl), c->stream), "reset control block");
+  CK(launch_preprocess(static_cast<FrameUniforms*>(c->frame.p), c->n,
+                       static_cast<float4*>(c->pos.p), static_cast<float4*>(c->scale.p),
+                       static_cast<float4*>(c->rot.p), static_cast<float4*>(c->color.p),
+                       c->sh_degree ? static_cast<float*>(c->sh.p) : nullptr, c->sh_degree,
+                       static_cast<gs3d_projected_splat*>(c->proj.p),
+                       static_cast<uint32_t*>(c->counts.p), &ctrl_of(c)->error, c->stream),
+     "preprocess");
+  return GS3D_OK;
+}
+
+int gs3d_prefix_scan(gs3d_ctx* c) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  TRY(require_frame(c, "prefix_scan"));
+  TRY(set_device(c));
+  CK(cudaMemsetAsync(&ctrl_of(c)->scan_tile_counter, 0, sizeof(uint32_t), c->stream),
+     "reset scan ticket");
+  c->scan_epoch = (c->scan_epoch % ((1u << 30) - 1)) + 1;  // 1 .. 2^30-1, never 0
+  CK(launch_scan(static_cast<uint32_t*>(c->counts.p), static_cast<uint32_t*>(c->offsets.p), c->n,
+                 static_cast<unsigned long long*>(c->scan_status.p),
+                 &ctrl_of(c)->scan_tile_counter, c->scan_epoch,
+                 static_cast<uint32_t*>(c->ref_counter.p), &ctrl_of(c)->error, c->stream),
+     "prefix scan");
+  return GS3D_OK;
+}
+
+int gs3d_emit_tile_refs(gs3d_ctx* c) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  TRY(require_frame(c, "emit_tile_refs"));
+  TRY(set_device(c));
+  CK(launch_emit(static_cast<FrameUniforms*>(c->frame.p), c->n,
+                 static_cast<gs3d_projected_splat*>(c->proj.p),
+                 static_cast<uint32_t*>(c->offsets.p), static_cast<uint32_t*>(c->ref_counter.p),
+                 c->capacity, static_cast<uint2*>(c->keys_a.p),
+                 static_cast<uint32_t*>(c->vals_a.p), &ctrl_of(c)->error, c->stream),
+     "emit_tile_refs");
+  return GS3D_OK;
+}
+
+int gs3d_radix_sort(gs3d_ctx* c) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  TRY(require_frame(c, "radix_sort"));
+  TRY(set_device(c));
+  const SortPlan plan = make_sort_plan(c->tiles_x * c->tiles_y);
+  CK(launch_sort(plan, static_cast<uint32_t*>(c->ref_counter.p), c->capacity,
+                 static_cast<uint2*>(c->keys_a.p), static_cast<uint32_t*>(c->vals_a.p),
+                 static_cast<uint2*>(c->keys_b.p), static_cast<uint32_t*>(c->vals_b.p),
+                 static_cast<uint32_t*>(c->sort_status.p), ctrl_of(c), c->sm_count, c->stream),
+     "radix sort");
+  if (plan.passes % 2) {  // sorted data ended in the B buffers: rename
+    std::swap(c->keys_a, c->keys_b);
+    std::swap(c->vals_a, c->vals_b);
+  }
+  return GS3D_OK;
+}
+
+int gs3d_identify_tile_ranges(gs3d_ctx* c) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  TRY(require_frame(c, "identify_tile_ranges"));
+  TRY(set_device(c));
+  CK(launch_identify(static_cast<uint2*>(c->keys_a.p), static_cast<uint32_t*>(c->ref_counter.p),
+                     c->capacity, c->tiles_x * c->tiles_y,
+                     static_cast<uint32_t*>(c->tile_offsets.p), &ctrl_of(c)->error, c->sm_count,
+                     c->stream),
+     "identify_tile_ranges");
+  return GS3D_OK;
+}
+
+int gs3d_rasterize_tiles(gs3d_ctx* c) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  TRY(require_frame(c, "rasterize_tiles"));
+  TRY(set_device(c));
+  CK(launch_raster(static_cast<FrameUniforms*>(c->frame.p), c->tiles_x, c->tiles_y, c->tile_w,
+                   c->tile_h, static_cast<gs3d_projected_splat*>(c->proj.p),
+                   static_cast<uint32_t*>(c->tile_offsets.p),
+                   static_cast<uint32_t*>(c->vals_a.p), static_cast<uint2*>(c->image.p),
+                   static_cast<uint32_t*>(c->tile_costs.p), c->stream),
+     "rasterize_tiles");
+  return GS3D_OK;
+}
+
+int gs3d_rebin(gs3d_ctx* c, const gs3d_camera* cam, uint32_t width, uint32_t height) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  TRY(gs3d_set_camera(c, cam, width, height));
+  TRY(gs3d_preprocess(c));
+  TRY(gs3d_prefix_scan(c));
+  TRY(gs3d_emit_tile_refs(c));
+  TRY(gs3d_radix_sort(c));
+  TRY(gs3d_identify_tile_ranges(c));
+  TRY(gs3d_rasterize_tiles(c));
+  return GS3D_OK;
+}
+
+int gs3d_synchronize(gs3d_ctx* c) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  TRY(set_device(c));
+  return sync_and_check(c);
+}
+
+static DevBuf* named(gs3d_ctx* c, gs3d_buffer which) {
+  switch (which) {
+    case GS3D_BUF_SPLAT_POSITIONS: return &c->pos;
+    case GS3D_BUF_SPLAT_SCALES: return &c->scale;
+    case GS3D_BUF_SPLAT_ROTATIONS: return &c->rot;
+    case GS3D_BUF_SPLAT_COLORS: return &c->color;
+    case GS3D_BUF_SPLAT_SH_REST: return &c->sh;
+    case GS3D_BUF_PROJECTED_SPLATS: return &c->proj;
+    case GS3D_BUF_SPLAT_REF_COUNTS: return &c->counts;
+    case GS3D_BUF_SPLAT_REF_OFFSETS: return &c->offsets;
+    case GS3D_BUF_REF_COUNTER: return &c->ref_counter;
+    case GS3D_BUF_SORT_KEYS_A: return &c->keys_a;
+    case GS3D_BUF_SORT_VALUES_A: return &c->vals_a;
+    case GS3D_BUF_SORT_KEYS_B: return &c->keys_b;
+    case GS3D_BUF_SORT_VALUES_B: return &c->vals_b;
+    case GS3D_BUF_TILE_OFFSETS: return &c->tile_offsets;
+    case GS3D_BUF_SPLAT_TARGET: return &c->image;
+    case GS3D_BUF_TILE_COSTS: return &c->tile_costs;
+    default: return nullptr;
+  }
+}
+
+int gs3d_buffer_info(gs3d_ctx* c, gs3d_buffer which, void** ptr, size_t* bytes) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  DevBuf* b = named(c, which);
+  if (!b) return fail(c, GS3D_ERR_INVALID_ARG, "unknown buffer %d", (int)which);
+  if (ptr) *ptr = b->p;
+  if (bytes) *bytes = b->bytes;
+  return GS3D_OK;
+}
+
+int gs3d_read_buffer(gs3d_ctx* c, gs3d_buffer which, void* dst, size_t bytes) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  DevBuf* b = named(c, which);
+  if (!b) return fail(c, GS3D_ERR_INVALID_ARG, "unknown buffer %d", (int)which);
+  if (bytes > b->bytes)
+    return fail(c, GS3D_ERR_INVALID_ARG, "read of %zu bytes from a %zu-byte buffer", bytes,
+                b->bytes);
+  if (bytes && !dst) return fail(c, GS3D_ERR_INVALID_ARG, "null destination");
+  TRY(set_device(c));
+  TRY(sync_and_check(c));
+  if (bytes) CK(cudaMemcpy(dst, b->p, bytes, cudaMemcpyDeviceToHost), "copy-out");
+  return GS3D_OK;
+}
+
+int gs3d_write_buffer(gs3d_ctx* c, gs3d_buffer which, const void* src, size_t bytes) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  DevBuf* b = named(c, which);
+  if (!b) return fail(c, GS3D_ERR_INVALID_ARG, "unknown buffer %d", (int)which);
+  if (bytes > b->bytes)
+    return fail(c, GS3D_ERR_INVALID_ARG, "write of %zu bytes into a %zu-byte buffer", bytes,
+                b->bytes);
+  if (bytes && !src) return fail(c, GS3D_ERR_INVALID_ARG, "null source");
+  TRY(set_device(c));
+  CK(cudaStreamSynchronize(c->stream), "synchronize before copy-in");
+  if (bytes) CK(cudaMemcpy(b->p, src, bytes, cudaMemcpyHostToDevice), "copy-in");
+  return GS3D_OK;
+}
+
+int gs3d_copy_buffer_async(gs3d_ctx* c, gs3d_buffer which, void* dst, size_t bytes) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  DevBuf* b = named(c, which);
+  if (!b) return fail(c, GS3D_ERR_INVALID_ARG, "unknown buffer %d", (int)which);
+  if (bytes > b->bytes)
+    return fail(c, GS3D_ERR_INVALID_ARG, "copy of %zu bytes from a %zu-byte buffer", bytes,
+                b->bytes);
+  if (bytes && !dst) return fail(c, GS3D_ERR_INVALID_ARG, "null destination");
+  TRY(set_device(c));
+  if (bytes)
+    CK(cudaMemcpyAsync(dst, b->p, bytes, cudaMemcpyDeviceToHost, c->stream), "async copy-out");
+  return GS3D_OK;
+}
+
+int gs3d_ref_count(gs3d_ctx* c, uint32_t* out) {
+  if (!c || !out) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
+  return gs3d_read_buffer(c, GS3D_BUF_REF_COUNTER, out, sizeof(uint32_t));
+}
+
+int gs3d_read_tile_counts(gs3d_ctx* c, uint32_t* counts, size_t n) {
+  if (!c || !counts) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
+  if (!c->have_camera) return fail(c, GS3D_ERR_STATE, "no frame");
+  const size_t tiles = (size_t)c->tiles_x * c->tiles_y;
+  if (n < tiles) return fail(c, GS3D_ERR_INVALID_ARG, "need room for %zu tiles", tiles);
+  uint32_t* off = new (std::nothrow) uint32_t[tiles + 1];
+  if (!off) return fail(c, GS3D_ERR_OOM, "host allocation");
+  const int rc = gs3d_read_buffer(c, GS3D_BUF_TILE_OFFSETS, off, (tiles + 1) * 4);
+  if (rc == GS3D_OK)
+    for (size_t t = 0; t < tiles; ++t) counts[t] = off[t + 1] >= off[t] ? off[t + 1] - off[t] : 0;
+  delete[] off;
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,95 @@
+// emit.cu - stage 3 of the rebin: one (key, value) pair per (splat, tile).
+//
+// Same output as src/shaders/compute/emit_tile_refs.wgsl:57-79: for each
+// valid splat, keys[off + k] = {hi: ty * tiles_x + tx, lo: bits(-depth)} and
+// values[off + k] = splat id, tiles in row-major order of the splat's tile
+// rectangle.  The reference loops per splat (one thread writes a whole
+// footprint, divergent for large splats); here a block owns 256 consecutive
+// splats, whose refs form one contiguous range of the output, and its threads
+// walk that range with unit stride, each ref finding its splat by a binary
+// search over the block's offsets in shared memory.  Stores are therefore
+// fully coalesced whatever the footprint distribution.
+//
+// Capacity: the reference writes past maxRefs relying on robust buffer
+// access (emit_tile_refs.wgsl:68-77).  Here the live count is compared with
+// the key capacity first; on overflow nothing is written and
+// DEVERR_CAPACITY is latched.
+#include "gs3d_internal.cuh"
+
+namespace gs3d {
+namespace {
+
+constexpr int kThreads = 256;
+
+__global__ void __launch_bounds__(kThreads)
+    emit_kernel(const FrameUniforms* __restrict__ fu, uint32_t n,
+                const gs3d_projected_splat* __restrict__ proj, const uint32_t* __restrict__ offsets,
+                const uint32_t* __restrict__ ref_counter, uint32_t capacity,
+                uint2* __restrict__ keys, uint32_t* __restrict__ values,
+                uint32_t* __restrict__ err) {
+  __shared__ uint32_t s_off[kThreads + 1];
+  __shared__ uint32_t s_tminx[kThreads], s_tminy[kThreads], s_w[kThreads], s_cnt[kThreads];
+  __shared__ uint32_t s_lo[kThreads];
+
+  const uint32_t total = *ref_counter;
+  if (total > capacity) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) latch_error(err, DEVERR_CAPACITY);
+    return;
+  }
+  const uint32_t first = blockIdx.x * kThreads;
+  const uint32_t i = first + threadIdx.x;
+  const uint32_t tiles_x = __ldg(&fu->tile_count[0]);
+
+  if (i < n) {
+    const float4 r0 = __ldg(reinterpret_cast<const float4*>(proj + i));
+    const uint32_t valid = __ldg(&proj[i].valid);
+    const uint4 r3 = __ldg(reinterpret_cast<const uint4*>(proj + i) + 3);
+    const uint32_t w = r3.z - r3.x + 1u, h = r3.w - r3.y + 1u;
+    s_off[threadIdx.x] = __ldg(offsets + i);
+    s_tminx[threadIdx.x] = r3.x;
+    s_tminy[threadIdx.x] = r3.y;
+    s_w[threadIdx.x] = w;
+    s_cnt[threadIdx.x] = valid ? w * h : 0u;
+    s_lo[threadIdx.x] = __float_as_uint(-r0.z);
+  }
+  const uint32_t last = min(n, first + kThreads);  // one past the block's last splat
+  if (threadIdx.x == 0) s_off[last - first] = __ldg(offsets + last);
+  __syncthreads();
+
+  const uint32_t nloc = last - first;
+  const uint32_t begin = s_off[0], end = s_off[nloc];
+  if (end < begin || end > total) {  // inconsistent offsets: write nothing
+    if (threadIdx.x == 0) latch_error(err, DEVERR_RANGE);
+    return;
+  }
+  for (uint32_t j = begin + threadIdx.x; j < end; j += kThreads) {
+    // largest s with s_off[s] <= j (ties: the last splat with that offset)
+    uint32_t lo = 0, hi = nloc;  // invariant: s_off[lo] <= j < s_off[hi]
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (s_off[mid] <= j) lo = mid; else hi = mid;
+    }
+    const uint32_t k = j - s_off[lo];
+    if (k >= s_cnt[lo]) continue;  // not covered by the splat's rectangle
+    const uint32_t w = s_w[lo];
+    const uint32_t ty = s_tminy[lo] + k / w;
+    const uint32_t tx = s_tminx[lo] + k % w;
+    keys[j] = make_uint2(ty * tiles_x + tx, s_lo[lo]);
+    values[j] = first + lo;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_emit(const FrameUniforms* d_frame, uint32_t n,
+                        const gs3d_projected_splat* proj, const uint32_t* offsets,
+                        const uint32_t* ref_counter, uint32_t capacity, uint2* keys,
+                        uint32_t* values, uint32_t* err, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const uint32_t blocks = (n + kThreads - 1) / kThreads;
+  emit_kernel<<<blocks, kThreads, 0, s>>>(d_frame, n, proj, offsets, ref_counter, capacity, keys,
+                                          values, err);
+  return cudaGetLastError();
+}
+
+}  // namespace gs3d

@@ -1,0 +1,173 @@
+// gs3d_internal.cuh - device-side structures and helpers shared by the
+// sm_103a kernels of the rebin library.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gs3d.h"
+
+namespace gs3d {
+
+// ---------------------------------------------------------------------------
+// Device-resident per-frame uniforms: CameraUniforms + SplatBinningUniforms +
+// TileUniforms of the reference (preprocess_splats.wgsl:1-16,
+// rasterize_tiles.wgsl:12-15), written once per rebin by one H2D copy.
+struct FrameUniforms {
+  gs3d_camera cam;          // 288 B
+  uint32_t tile_count[2];   // tiles_x, tiles_y
+  uint32_t splat_count;
+  uint32_t num_tiles;
+  float inv_tile[2];        // f32(1.0 / tile size), GaussianSplatRenderer.ts:1127-1128
+  uint32_t viewport[2];     // width, height
+  uint32_t tile_size[2];
+  uint32_t tile_base;       // first global tile id of this view (batched path)
+  uint32_t pad;
+};
+static_assert(sizeof(FrameUniforms) % 16 == 0, "FrameUniforms is copied as 16-byte words");
+
+// Device error latch bits (read and cleared by gs3d_synchronize).
+enum : uint32_t {
+  DEVERR_CAPACITY = 1u,  // live ref count exceeded key capacity: nothing written
+  DEVERR_TIMEOUT = 2u,   // a bounded look-back spin gave up
+  DEVERR_RANGE = 4u,     // a key's tile id was outside tile_offsets
+};
+
+constexpr int kMaxSortPasses = 8;
+constexpr int kRadixBins = 256;
+
+// Per-frame control block, zeroed at the start of every rebin.
+struct Ctrl {
+  uint32_t error;
+  uint32_t scan_tile_counter;
+  uint32_t sort_part_counter[kMaxSortPasses];
+  uint32_t pad[6];
+  uint32_t sort_hist[kMaxSortPasses][kRadixBins];  // global digit histograms
+};
+
+// Bounded spins: a device wait gives up after this many polls (with
+// __nanosleep back-off this is on the order of a second), latches
+// DEVERR_TIMEOUT and returns instead of hanging the GPU.
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+// ---------------------------------------------------------------------------
+// PTX helpers
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+// 16-byte global->shared asynchronous copy (L2 only).
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(smem_dst)),
+               "l"(gmem_src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// mbarrier + bulk (TMA, non-tensor) copy helpers.
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// Bulk copy global -> shared, completion signalled on `bar` (bytes % 16 == 0,
+// both addresses 16-byte aligned).
+__device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gmem_src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(smem_dst)),
+      "l"(gmem_src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// Bounded parity wait; returns false if the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (i > 64) __nanosleep(64);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void latch_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }
+
+// Live ref count guarded by capacity: a count above capacity was latched as
+// DEVERR_CAPACITY by emit and every later stage treats it as zero.
+__device__ __forceinline__ uint32_t live_refs(const uint32_t* ref_counter, uint32_t capacity) {
+  const uint32_t r = *ref_counter;
+  return r > capacity ? 0u : r;
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launchers (one translation unit per stage).
+struct SortPlan {
+  int passes;                    // number of 8-bit digit passes
+  int word[kMaxSortPasses];      // 0 = hi (tile id), 1 = lo (depth bits)
+  int shift[kMaxSortPasses];
+};
+SortPlan make_sort_plan(uint32_t num_tiles);
+
+cudaError_t launch_preprocess(const FrameUniforms* d_frame, uint32_t n, const float4* pos,
+                              const float4* scale, const float4* rot, const float4* color,
+                              const float* sh_rest, uint32_t sh_degree,
+                              gs3d_projected_splat* out, uint32_t* counts, uint32_t* err,
+                              cudaStream_t s);
+cudaError_t launch_scan(const uint32_t* counts, uint32_t* offsets, uint32_t n,
+                        unsigned long long* status, uint32_t* tile_counter, uint32_t epoch,
+                        uint32_t* total_out, uint32_t* err, cudaStream_t s);
+size_t scan_status_words(uint32_t n);
+cudaError_t launch_emit(const FrameUniforms* d_frame, uint32_t n,
+                        const gs3d_projected_splat* proj, const uint32_t* offsets,
+                        const uint32_t* ref_counter, uint32_t capacity, uint2* keys,
+                        uint32_t* values, uint32_t* err, cudaStream_t s);
+cudaError_t launch_sort(const SortPlan& plan, const uint32_t* ref_counter, uint32_t capacity,
+                        uint2* keys_a, uint32_t* vals_a, uint2* keys_b, uint32_t* vals_b,
+                        uint32_t* status, Ctrl* ctrl, int sm_count, cudaStream_t s);
+size_t sort_status_words(uint32_t capacity, int passes);
+cudaError_t launch_identify(const uint2* keys, const uint32_t* ref_counter, uint32_t capacity,
+                            uint32_t num_tiles, uint32_t* tile_offsets, uint32_t* err,
+                            int sm_count, cudaStream_t s);
+cudaError_t launch_raster(const FrameUniforms* d_frame, uint32_t tiles_x, uint32_t tiles_y,
+                          uint32_t tile_w, uint32_t tile_h, const gs3d_projected_splat* proj,
+                          const uint32_t* tile_offsets, const uint32_t* values, uint2* image,
+                          uint32_t* tile_costs, cudaStream_t s);
+
+}  // namespace gs3d

@@ -1,0 +1,334 @@
+// sort.cu - stage 4 of the rebin: stable LSD radix sort of the 64-bit
+// (tile | depth) keys with their splat-id values.
+//
+// The reference runs eight 8-bit passes, each as three dispatch groups
+// (radix_histogram.wgsl, a recursive Blelloch scan, radix_scatter.wgsl with a
+// serial lane-0 rank).  This file implements the onesweep scheme instead:
+//
+//   1. one histogram kernel reads every key once and builds the 256-bin
+//      histogram of every digit place that is sorted (and clears the
+//      look-back status of the passes);
+//   2. one kernel per pass: a persistent CTA claims 4096-key partitions in
+//      order, ranks its keys stably with warp ballots (8 ballots give each
+//      lane the mask of lanes holding the same 8-bit digit) and per-warp
+//      shared-memory histograms, publishes its per-digit counts, resolves
+//      each digit's global offset by decoupled look-back over earlier
+//      partitions, reorders the partition in shared memory and writes each
+//      digit run out contiguously.
+//
+// Digit places above the highest set bit of (tile count - 1) are always zero
+// and are skipped: 4 depth passes + ceil(tile bits / 8) tile passes instead of
+// 8.  Passes alternate A->B->A; with an odd pass count the sorted result ends
+// in the B buffers and the host swaps the buffer names.
+//
+// The order produced is identical to the reference's: lexicographic
+// (tile id, depth bits, emit position), since every pass is a stable
+// counting sort on one digit.
+#include "gs3d_internal.cuh"
+
+namespace gs3d {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kItems = 16;
+constexpr uint32_t kPart = kThreads * kItems;  // 4096 keys per partition
+constexpr uint32_t kFlagAgg = 1u, kFlagInc = 2u;
+constexpr uint32_t kValueMask = (1u << 30) - 1u;
+constexpr size_t kPassSmem = (size_t)kPart * (sizeof(uint2) + sizeof(uint32_t)) +
+                             (size_t)kWarps * kRadixBins * sizeof(uint32_t);
+
+struct PassDev {
+  int word[kMaxSortPasses];
+  int shift[kMaxSortPasses];
+};
+
+__device__ __forceinline__ uint32_t digit_of(uint2 k, int word, int shift) {
+  return ((word ? k.y : k.x) >> shift) & 0xffu;
+}
+
+__device__ __forceinline__ uint32_t warp_inclusive(uint32_t x, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+// Exclusive scan of one value per thread over a 256-thread block.
+__device__ __forceinline__ uint32_t block_exclusive_256(uint32_t x, uint32_t* s_wsum) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t inc = warp_inclusive(x, lane);
+  __syncthreads();  // s_wsum may still be read from a previous call
+  if (lane == 31) s_wsum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t w = lane < kWarps ? s_wsum[lane] : 0u;
+    const uint32_t wi = warp_inclusive(w, lane);
+    if (lane < kWarps) s_wsum[lane] = wi - w;
+  }
+  __syncthreads();
+  return s_wsum[warp] + inc - x;
+}
+
+// Mask of lanes whose 8-bit digit equals this lane's.
+__device__ __forceinline__ uint32_t match_digit8(uint32_t d) {
+  uint32_t peers = 0xffffffffu;
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const uint32_t bit = (d >> b) & 1u;
+    const uint32_t bal = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? bal : ~bal;
+  }
+  return peers;
+}
+
+// Histogram of every sorted digit place + clear of the look-back status.
+__global__ void __launch_bounds__(kThreads)
+    sort_histogram_kernel(const uint2* __restrict__ keys, const uint32_t* __restrict__ ref_counter,
+                          uint32_t capacity, int passes, PassDev pd, uint32_t* __restrict__ g_hist,
+                          uint32_t* __restrict__ status, size_t status_stride) {
+  __shared__ uint32_t s_hist[kMaxSortPasses][kRadixBins];
+  for (int k = threadIdx.x; k < kMaxSortPasses * kRadixBins; k += kThreads)
+    (&s_hist[0][0])[k] = 0u;
+  __syncthreads();
+
+  const uint32_t R = live_refs(ref_counter, capacity);
+  const size_t parts = (R + kPart - 1) / kPart;
+  const size_t gtid = (size_t)blockIdx.x * kThreads + threadIdx.x;
+  const size_t gstride = (size_t)gridDim.x * kThreads;
+
+  // clear status words of the partitions this sort will use
+  const size_t words = parts * kRadixBins;
+  for (size_t k = gtid; k < words * passes; k += gstride) {
+    const size_t p = k / words, o = k - p * words;
+    status[p * status_stride + o] = 0u;
+  }
+
+  const int lane = threadIdx.x & 31;
+  for (size_t base = (size_t)blockIdx.x * kThreads; base < R; base += gstride) {
+    const size_t idx = base + threadIdx.x;
+    const bool in = idx < R;
+    const uint2 k = in ? __ldg(keys + idx) : make_uint2(0u, 0u);
+    for (int p = 0; p < passes; ++p) {
+      const uint32_t d = digit_of(k, pd.word[p], pd.shift[p]);
+      const uint32_t act = __ballot_sync(0xffffffffu, in);
+      if (in) {
+        const uint32_t peers = __match_any_sync(act, d);
+        if ((__ffs(peers) - 1) == lane) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
+      }
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < passes * kRadixBins; k += kThreads) {
+    const uint32_t v = (&s_hist[0][0])[k];
+    if (v) atomicAdd(g_hist + k, v);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 2)
+    onesweep_kernel(const uint2* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                    uint2* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                    const uint32_t* __restrict__ ref_counter, uint32_t capacity, int word,
+                    int shift, const uint32_t* __restrict__ hist, uint32_t* __restrict__ status,
+                    uint32_t* __restrict__ part_counter, uint32_t* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint2* s_keys = reinterpret_cast<uint2*>(smem);
+  uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + kPart);
+  uint32_t* s_whist = s_vals + kPart;  // [kWarps][256]
+  __shared__ uint32_t s_bucket[kRadixBins], s_dstart[kRadixBins], s_dest[kRadixBins];
+  __shared__ uint32_t s_wsum[kWarps];
+  __shared__ uint32_t s_part;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t R = live_refs(ref_counter, capacity);
+  const uint32_t num_parts = (R + kPart - 1) / kPart;
+
+  // global bucket bases of this digit place
+  s_bucket[tid] = block_exclusive_256(__ldg(hist + tid), s_wsum);
+
+  while (true) {
+    __syncthreads();  // previous partition fully written out
+    if (tid == 0) s_part = atomicAdd(part_counter, 1u);
+    for (int k = tid; k < kWarps * kRadixBins; k += kThreads) s_whist[k] = 0u;
+    __syncthreads();
+    const uint32_t part = s_part;
+    if (part >= num_parts) break;
+    const uint32_t base = part * kPart;
+    const uint32_t count = min(kPart, R - base);
+
+    // ---- load (warp-striped: lane-contiguous, coalesced) ----
+    uint2 key[kItems];
+    uint32_t val[kItems];
+    uint32_t dr[kItems];  // digit | rank-in-warp << 8
+    const uint32_t wbase = base + warp * (32u * kItems);
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const uint32_t idx = wbase + i * 32u + lane;
+      if (idx < R) {
+        key[i] = __ldg(keys_in + idx);
+        val[i] = __ldg(vals_in + idx);
+      } else {
+        key[i] = make_uint2(0xffffffffu, 0xffffffffu);  // digit 255, ranked last
+        val[i] = 0u;
+      }
+    }
+    // ---- stable rank within the warp ----
+    uint32_t* wh = s_whist + warp * kRadixBins;
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const uint32_t d = digit_of(key[i], word, shift);
+      const uint32_t peers = match_digit8(d);
+      const uint32_t prior = wh[d];
+      __syncwarp();
+      if ((__ffs(peers) - 1) == lane) wh[d] = prior + __popc(peers);
+      __syncwarp();
+      dr[i] = d | ((prior + __popc(peers & lt)) << 8);
+    }
+    __syncthreads();
+
+    // ---- per digit (thread = digit): warp offsets, partition totals ----
+    uint32_t run = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      const uint32_t t = s_whist[w * kRadixBins + tid];
+      s_whist[w * kRadixBins + tid] = run;
+      run += t;
+    }
+    const uint32_t pub = (tid == kRadixBins - 1) ? run - (kPart - count) : run;
+    uint32_t* st = status + (size_t)part * kRadixBins + tid;
+    st_relaxed_u32(st, ((part == 0 ? kFlagInc : kFlagAgg) << 30) | pub);
+    const uint32_t dstart = block_exclusive_256(run, s_wsum);  // includes a barrier
+    s_dstart[tid] = dstart;
+    __syncthreads();
+
+    // ---- reorder the partition in shared memory ----
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const uint32_t d = dr[i] & 0xffu;
+      const uint32_t pos = s_dstart[d] + s_whist[warp * kRadixBins + d] + (dr[i] >> 8);
+      s_keys[pos] = key[i];
+      s_vals[pos] = val[i];
+    }
+
+    // ---- decoupled look-back, one thread per digit ----
+    uint32_t excl = 0;
+    bool ok = true;
+    if (part > 0) {
+      for (int pp = (int)part - 1; pp >= 0; --pp) {
+        const uint32_t* ps = status + (size_t)pp * kRadixBins + tid;
+        uint32_t w = ld_relaxed_u32(ps);
+        uint32_t spins = 0;
+        while ((w >> 30) == 0u) {
+          if (++spins > kSpinLimit) break;
+          if (spins > 16) __nanosleep(32);
+          w = ld_relaxed_u32(ps);
+        }
+        if ((w >> 30) == 0u) {
+          ok = false;
+          break;
+        }
+        excl += w & kValueMask;
+        if ((w >> 30) == kFlagInc) break;
+      }
+      st_relaxed_u32(st, (kFlagInc << 30) | ((excl + pub) & kValueMask));
+    }
+    s_dest[tid] = s_bucket[tid] + excl - dstart;
+    const int all_ok = __syncthreads_and(ok);
+    if (!all_ok) {
+      if (tid == 0) latch_error(err, DEVERR_TIMEOUT);
+      continue;  // nothing written for this partition
+    }
+
+    // ---- write each digit run contiguously ----
+    for (uint32_t j = tid; j < count; j += kThreads) {
+      const uint2 k = s_keys[j];
+      const uint32_t dst = s_dest[digit_of(k, word, shift)] + j;
+      if (dst < R) {
+        keys_out[dst] = k;
+        vals_out[dst] = s_vals[j];
+      } else {
+        latch_error(err, DEVERR_RANGE);
+      }
+    }
+  }
+}
+
+int g_onesweep_blocks_per_sm = 0;
+
+}  // namespace
+
+SortPlan make_sort_plan(uint32_t num_tiles) {
+  SortPlan p{};
+  int n = 0;
+  for (int s = 0; s < 32; s += 8) {  // depth bits (lo word)
+    p.word[n] = 1;
+    p.shift[n] = s;
+    ++n;
+  }
+  const uint32_t max_tile = num_tiles > 0 ? num_tiles - 1 : 0;
+  const int bits = max_tile ? 32 - __builtin_clz(max_tile) : 0;
+  for (int s = 0; s < bits; s += 8) {  // tile-id bits (hi word)
+    p.word[n] = 0;
+    p.shift[n] = s;
+    ++n;
+  }
+  p.passes = n;
+  return p;
+}
+
+size_t sort_status_words(uint32_t capacity, int passes) {
+  const size_t parts = ((size_t)capacity + kPart - 1) / kPart + 1;
+  return parts * kRadixBins * (size_t)passes;
+}
+
+cudaError_t launch_sort(const SortPlan& plan, const uint32_t* ref_counter, uint32_t capacity,
+                        uint2* keys_a, uint32_t* vals_a, uint2* keys_b, uint32_t* vals_b,
+                        uint32_t* status, Ctrl* ctrl, int sm_count, cudaStream_t s) {
+  if (g_onesweep_blocks_per_sm == 0) {
+    cudaError_t e = cudaFuncSetAttribute(onesweep_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kPassSmem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, onesweep_kernel, kThreads,
+                                                      kPassSmem);
+    if (e != cudaSuccess) return e;
+    g_onesweep_blocks_per_sm = per_sm > 0 ? per_sm : 1;
+  }
+  // counters and histograms for this sort
+  cudaError_t e = cudaMemsetAsync(ctrl->sort_part_counter, 0,
+                                  sizeof(ctrl->sort_part_counter) + sizeof(ctrl->pad) +
+                                      sizeof(ctrl->sort_hist),
+                                  s);
+  if (e != cudaSuccess) return e;
+  const size_t parts_cap = ((size_t)capacity + kPart - 1) / kPart + 1;
+  const size_t stride = parts_cap * kRadixBins;
+  PassDev pd{};
+  for (int p = 0; p < plan.passes; ++p) {
+    pd.word[p] = plan.word[p];
+    pd.shift[p] = plan.shift[p];
+  }
+  sort_histogram_kernel<<<sm_count * 4, kThreads, 0, s>>>(keys_a, ref_counter, capacity,
+                                                          plan.passes, pd, &ctrl->sort_hist[0][0],
+                                                          status, stride);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const size_t max_grid = (size_t)sm_count * g_onesweep_blocks_per_sm;
+  const int grid = (int)std::min(max_grid, parts_cap);
+  for (int p = 0; p < plan.passes; ++p) {
+    const bool even = (p % 2) == 0;
+    onesweep_kernel<<<grid, kThreads, kPassSmem, s>>>(
+        even ? keys_a : keys_b, even ? vals_a : vals_b, even ? keys_b : keys_a,
+        even ? vals_b : vals_a, ref_counter, capacity, plan.word[p], plan.shift[p],
+        ctrl->sort_hist[p], status + (size_t)p * stride, &ctrl->sort_part_counter[p],
+        &ctrl->error);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace gs3d

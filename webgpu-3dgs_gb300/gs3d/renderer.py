@@ -1,0 +1,282 @@
+"""Host mirror of the reference renderer's plug-in surface over libgs3d.
+
+`GaussianSplatRenderer` keeps the method names and argument meaning of
+src/renderers/GaussianSplatRenderer.ts (init, render, rebin, setTileSize,
+setAlwaysRebin, getTileCount, getTileSize, readTileCounts) and `SceneSyncer`
+those of src/SceneSyncer.ts (setSplatData).  A WebGPU command encoder and
+swapchain texture do not exist here: `render` takes a `RenderFrameInfo` that
+carries the viewport size, the camera and its version counter, and the splat
+target is a headless rgba16float device buffer (readImage copies it out).
+
+Errors: the reference throws on configuration bugs and surfaces WebGPU
+validation errors asynchronously; here every library failure raises
+`Gs3dError` carrying the C status code and the library's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import Config_t, Gs3dError
+from .camera import Camera, camera_struct
+from .scenes import GaussianSplatData
+
+PROJ_DTYPE = np.dtype([
+    ("mean_px", "<f4", (2,)), ("depth", "<f4"), ("radius_px", "<f4"),
+    ("conic", "<f4", (3,)), ("opacity", "<f4"),
+    ("color", "<f4", (3,)), ("valid", "<u4"),
+    ("tile_min", "<u4", (2,)), ("tile_max", "<u4", (2,)),
+])
+
+
+@dataclass
+class Scene:
+    """src/Scene.ts: tile pixel size and the splat data."""
+    tiles: list = field(default_factory=lambda: [16, 16])
+    splats: GaussianSplatData | None = None
+
+
+@dataclass
+class RenderFrameInfo:
+    """src/renderers/IRenderer.ts:1-8 without the WebGPU textures."""
+    width: int
+    height: int
+    camera: Camera | np.ndarray  # a Camera or its 72-float uniform block
+    cameraVersion: int = 0
+
+
+def _check(lib, ctx, rc: int):
+    if rc != _lib.OK:
+        msg = lib.gs3d_last_error(ctx) if ctx else b"no context"
+        raise Gs3dError(rc, (msg or b"").decode(errors="replace"))
+
+
+class GaussianSplatRenderer:
+    def __init__(self, scene: Scene, device: int = 0, stream: int | None = None):
+        self.scene = scene
+        self.device = device
+        self.stream = stream
+        self.ctx = None
+        self.lib = None
+        self.alwaysRebin = False
+        self.lastSplatCount = -1
+        self.lastViewport = (-1, -1)
+        self.lastCameraVersion = -1
+        self.tileCountX = self.tileCountY = 0
+        self.tileSizeX, self.tileSizeY = scene.tiles
+        self.viewport = (0, 0)
+
+    # ---- lifetime (GaussianSplatRenderer.init, :331-471) -------------------
+    def init(self, format: str = "rgba16float") -> None:
+        if format != "rgba16float":
+            raise ValueError("the splat target is rgba16float (GaussianSplatRenderer.ts:234)")
+        self.lib = _lib.load()
+        cfg = Config_t(self.device, int(self.scene.tiles[0]), int(self.scene.tiles[1]), 16,
+                       self.stream, 0)
+        ctx = C.c_void_p()
+        rc = self.lib.gs3d_create(C.byref(ctx), C.byref(cfg))
+        if rc != _lib.OK:
+            raise Gs3dError(rc, "gs3d_create failed (no sm_103 device, or the library "
+                                "was built for another architecture)")
+        self.ctx = ctx
+        self.tileSizeX, self.tileSizeY = self.setTileSize(*self.scene.tiles)
+
+    def destroy(self) -> None:
+        if self.ctx:
+            self.lib.gs3d_destroy(self.ctx)
+            self.ctx = None
+
+    def __enter__(self):
+        if self.ctx is None:
+            self.init()
+        return self
+
+    def __exit__(self, *exc):
+        self.destroy()
+
+    def _call(self, name, *args):
+        _check(self.lib, self.ctx, getattr(self.lib, name)(self.ctx, *args))
+
+    # ---- SceneSyncer.setSplatData (SceneSyncer.ts:25-38) -------------------
+    def setSplatData(self, data: GaussianSplatData | None = None) -> None:
+        data = data if data is not None else self.scene.splats
+        if data is None:
+            return
+        self.scene.splats = data
+        arrs = [np.ascontiguousarray(a, np.float32) for a in
+                (data.positions, data.scales, data.rotations, data.colors)]
+        for a in arrs:
+            if a.shape != (data.splatCount, 4):
+                raise ValueError("splat arrays must be (N, 4) float32")
+        sh = None
+        deg = int(data.sphericalHarmonicsDegree)
+        if deg > 0:
+            sh = np.ascontiguousarray(data.sphericalHarmonics, np.float32)
+            k = 3 * ((deg + 1) ** 2 - 1)
+            if sh.shape != (data.splatCount, k):
+                raise ValueError(f"sphericalHarmonics must be (N, {k}) for degree {deg}")
+        ptr = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        self._call("gs3d_set_splats", data.splatCount, *(ptr(a) for a in arrs), ptr(sh), deg, 0)
+        self.lastSplatCount = -1  # force a rebin
+
+    # ---- knobs ---------------------------------------------------------------
+    def setTileSize(self, x: int, y: int) -> tuple[int, int]:
+        ox, oy = C.c_uint32(), C.c_uint32()
+        self._call("gs3d_set_tile_size", int(x), int(y), C.byref(ox), C.byref(oy))
+        if (ox.value, oy.value) != (self.tileSizeX, self.tileSizeY):
+            self.lastViewport = (-1, -1)
+        self.tileSizeX, self.tileSizeY = ox.value, oy.value
+        self.scene.tiles = [ox.value, oy.value]
+        return ox.value, oy.value
+
+    def setAlwaysRebin(self, on: bool) -> None:
+        self.alwaysRebin = bool(on)
+
+    def getTileCount(self) -> tuple[int, int]:
+        return self.tileCountX, self.tileCountY
+
+    def getTileSize(self) -> tuple[int, int]:
+        return self.tileSizeX, self.tileSizeY
+
+    # ---- frame ---------------------------------------------------------------
+    @staticmethod
+    def _uniform(camera, width, height) -> np.ndarray:
+        if isinstance(camera, Camera):
+            return camera.getUniformData(width, height)
+        return np.ascontiguousarray(camera, np.float32)
+
+    def render(self, frame: RenderFrameInfo) -> bool:
+        """GaussianSplatRenderer.render (:1033-1098) up to the composite pass:
+        re-runs the rebin only when the camera, splat count or viewport
+        changed (or always-rebin is on).  Returns whether it rebinned."""
+        if self.scene.splats is None:
+            return False
+        n = self.scene.splats.splatCount
+        w, h = max(1, int(frame.width)), max(1, int(frame.height))
+        self.tileCountX = -(-w // self.tileSizeX)
+        self.tileCountY = -(-h // self.tileSizeY)
+        count_changed = n != self.lastSplatCount
+        self.lastSplatCount = n
+        viewport_changed = (w, h) != self.lastViewport
+        self.lastViewport = (w, h)
+        moved = frame.cameraVersion != self.lastCameraVersion
+        self.lastCameraVersion = frame.cameraVersion
+        if self.alwaysRebin or moved or count_changed or viewport_changed:
+            self.rebin(n, self.tileCountX, self.tileCountY, w, h,
+                       self._uniform(frame.camera, w, h))
+            return True
+        return False
+
+    def rebin(self, splatCount, tilesX, tilesY, viewportWidth, viewportHeight,
+              camera_uniform: np.ndarray, check: bool = True) -> None:
+        """rebin (:1104-1266): all six stages.  On a key-capacity overflow the
+        library grows its buffers and the rebin is issued again, so the
+        result is never truncated."""
+        cam = camera_struct(camera_uniform)
+        self.viewport = (viewportWidth, viewportHeight)
+        self.tileCountX, self.tileCountY = tilesX, tilesY
+        for _ in range(3):
+            self._call("gs3d_rebin", C.byref(cam), viewportWidth, viewportHeight)
+            if not check:
+                return
+            rc = self.lib.gs3d_synchronize(self.ctx)
+            if rc == _lib.ERR_CAPACITY:
+                continue
+            _check(self.lib, self.ctx, rc)
+            return
+        _check(self.lib, self.ctx, rc)
+
+    # ---- individual stages (for stage-wise parity) --------------------------
+    def setCamera(self, camera_uniform, width, height) -> None:
+        cam = camera_struct(camera_uniform)
+        self._call("gs3d_set_camera", C.byref(cam), int(width), int(height))
+        self.viewport = (int(width), int(height))
+        self.tileCountX = -(-int(width) // self.tileSizeX)
+        self.tileCountY = -(-int(height) // self.tileSizeY)
+
+    def preprocess(self):
+        self._call("gs3d_preprocess")
+
+    def prefixScan(self):
+        self._call("gs3d_prefix_scan")
+
+    def emitTileRefs(self):
+        self._call("gs3d_emit_tile_refs")
+
+    def radixSort(self):
+        self._call("gs3d_radix_sort")
+
+    def identifyTileRanges(self):
+        self._call("gs3d_identify_tile_ranges")
+
+    def rasterizeTiles(self):
+        self._call("gs3d_rasterize_tiles")
+
+    def synchronize(self) -> None:
+        self._call("gs3d_synchronize")
+
+    # ---- buffers ---------------------------------------------------------------
+    def refCount(self) -> int:
+        v = C.c_uint32()
+        self._call("gs3d_ref_count", C.byref(v))
+        return int(v.value)
+
+    def bufferInfo(self, name: str) -> tuple[int, int]:
+        p, b = C.c_void_p(), C.c_size_t()
+        self._call("gs3d_buffer_info", _lib.BUFFERS[name], C.byref(p), C.byref(b))
+        return int(p.value or 0), int(b.value)
+
+    def readBuffer(self, name: str, count: int | None = None) -> np.ndarray:
+        """Copies a named buffer out in the reference's layout."""
+        n = self.scene.splats.splatCount if self.scene.splats else 0
+        tiles = self.tileCountX * self.tileCountY
+        w, h = self.viewport
+        if name in ("sort_keys_a", "sort_values_a", "sort_keys_b", "sort_values_b"):
+            count = self.refCount() if count is None else count
+        shapes = {
+            "projected_splats": (PROJ_DTYPE, (n,)),
+            "splat_ref_counts": (np.uint32, (n,)),
+            "splat_ref_offsets": (np.uint32, (n + 1,)),
+            "ref_counter": (np.uint32, (1,)),
+            "sort_keys_a": (np.uint32, (count, 2)), "sort_keys_b": (np.uint32, (count, 2)),
+            "sort_values_a": (np.uint32, (count,)), "sort_values_b": (np.uint32, (count,)),
+            "tile_offsets": (np.uint32, (tiles + 1,)),
+            "splat_target": (np.float16, (h, w, 4)),
+            "tile_costs": (np.uint32, (tiles,)),
+        }
+        dtype, shape = shapes[name]
+        out = np.zeros(shape, dtype)
+        self._call("gs3d_read_buffer", _lib.BUFFERS[name], out.ctypes.data_as(C.c_void_p),
+                   out.nbytes)
+        return out
+
+    def writeBuffer(self, name: str, data: np.ndarray) -> None:
+        data = np.ascontiguousarray(data)
+        self._call("gs3d_write_buffer", _lib.BUFFERS[name], data.ctypes.data_as(C.c_void_p),
+                   data.nbytes)
+
+    def readImage(self) -> np.ndarray:
+        return self.readBuffer("splat_target")
+
+    def readTileCounts(self) -> np.ndarray:
+        """readTileCounts (:1278-1310): max(0, off[t+1] - off[t]) per tile."""
+        tiles = self.tileCountX * self.tileCountY
+        out = np.zeros(tiles, np.uint32)
+        self._call("gs3d_read_tile_counts", out.ctypes.data_as(C.c_void_p), tiles)
+        return out
+
+
+class SceneSyncer:
+    """src/SceneSyncer.ts: pushes the scene's splat SoA into the renderer."""
+
+    def __init__(self, scene: Scene, renderer: GaussianSplatRenderer):
+        self.scene = scene
+        self.renderer = renderer
+
+    def setSplatData(self) -> None:
+        if self.scene.splats is None:
+            return
+        self.renderer.setSplatData(self.scene.splats)
