@@ -116,13 +116,16 @@ def make_workload(n_views: int):
     return data, cams
 
 
-def algorithmic_bytes(n, R, tiles, passes, sh_floats):
-    """Bytes each stage must move at minimum (per view)."""
+def algorithmic_bytes(n, R, tiles, tile_passes, sh_floats, fused):
+    """Minimum bytes each stage must move for one view (inputs read once,
+    outputs written once), the numerator of the per-stage roofline."""
+    full_passes = 4 + tile_passes
     return {
-        "preprocess-splats": n * (64 + 4 * sh_floats) + n * (64 + 4),
-        "prefix-scan": 8 * n,
-        "emit-tile-refs": n * (24 + 4) + 12 * R,
-        "radix-sort": 8 * R + passes * 24 * R,
+        "preprocess-splats": n * (64 + 4 * sh_floats) + n * (64 + 4 + (8 if fused else 0)),
+        "depth-sort": 4 * n + 4 * 16 * n,
+        "prefix-scan": 12 * n if fused else 8 * n,
+        "emit-tile-refs": n * (4 + 24 + 4) + 12 * R if fused else n * (24 + 4) + 12 * R,
+        "radix-sort": tile_passes * 24 * R if fused else 8 * R + full_passes * 24 * R,
         "identify-tile-ranges": 4 * R + 4 * (tiles + 1),
         "rasterize-tiles": 44 * R + 8 * WIDTH * HEIGHT,
     }
@@ -154,8 +157,6 @@ def run_ours(args, rank, world):
                               ptr(data.rotations), ptr(data.colors),
                               ptr(data.sphericalHarmonics), 3, 0))
     cam_structs = [camera_struct(u) for u in cams]
-    stage_fns = [lib.gs3d_preprocess, lib.gs3d_prefix_scan, lib.gs3d_emit_tile_refs,
-                 lib.gs3d_radix_sort, lib.gs3d_identify_tile_ranges, lib.gs3d_rasterize_tiles]
 
     # first pass: size the key buffers (grow on overflow) and record ref counts
     refs = []
@@ -170,50 +171,47 @@ def run_ours(args, rank, world):
         check(lib.gs3d_ref_count(ctx, C.byref(r)))
         refs.append(r.value)
 
-    def one_step(events=None):
-        for v, cs in enumerate(cam_structs):
-            check(lib.gs3d_set_camera(ctx, C.byref(cs), WIDTH, HEIGHT))
-            for s, fn in enumerate(stage_fns):
-                if events is not None:
-                    events[v][s].record(stream)
-                check(fn(ctx))
-            if events is not None:
-                events[v][len(stage_fns)].record(stream)
-
-    for _ in range(args.warmup):
-        one_step()
-    check(lib.gs3d_synchronize(ctx))
-
-    ev = [[[torch.cuda.Event(enable_timing=True) for _ in range(len(stage_fns) + 1)]
-           for _ in cam_structs] for _ in range(args.steps)]
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(dev) as clocks:
-        start.record(stream)
-        for k in range(args.steps):
-            one_step(ev[k])
-        stop.record(stream)
+    def timed(stagewise: bool):
+        flags = _lib.FLAG_STAGE_TIMING | (_lib.FLAG_STAGEWISE_REBIN if stagewise else 0)
+        check(lib.gs3d_set_flags(ctx, flags))
+        for _ in range(args.warmup):
+            for cs in cam_structs:
+                check(lib.gs3d_rebin(ctx, C.byref(cs), WIDTH, HEIGHT))
+        check(lib.gs3d_synchronize(ctx))
+        check(lib.gs3d_read_stage_times(ctx, None, None))  # reset
+        start, stop = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+        if world > 1:
+            torch.distributed.barrier()
         torch.cuda.synchronize()
-    check(lib.gs3d_synchronize(ctx))
-    total_ms = start.elapsed_time(stop)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    stage_ms = np.zeros(len(stage_fns))
-    for k in range(args.steps):
-        for v in range(len(cam_structs)):
-            for s in range(len(stage_fns)):
-                stage_ms[s] += ev[k][v][s].elapsed_time(ev[k][v][s + 1])
+        with ClockSampler(dev) as clocks:
+            start.record(stream)
+            for _ in range(args.steps):
+                for cs in cam_structs:
+                    check(lib.gs3d_rebin(ctx, C.byref(cs), WIDTH, HEIGHT))
+            stop.record(stream)
+            torch.cuda.synchronize()
+        check(lib.gs3d_synchronize(ctx))
+        ms = (C.c_double * 7)()
+        cnt = (C.c_uint32 * 7)()
+        check(lib.gs3d_read_stage_times(ctx, ms, cnt))
+        check(lib.gs3d_set_flags(ctx, 0))
+        total = start.elapsed_time(stop)
+        if world > 1:
+            t = torch.tensor([total], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total = float(t.item())
+        views = args.steps * len(cam_structs)
+        per_stage = {name: (ms[i] / views, cnt[i] / views) for i, name in
+                     enumerate(_lib.STAGE_NAMES) if cnt[i]}
+        return total, per_stage, clocks.summary()
+
+    fused_ms, fused_stages, clocks = timed(False)
+    stagewise_ms, stagewise_stages, _ = timed(True)
     views = args.steps * len(cam_structs)
-    stage_ms /= views  # per view
 
     # ---- e2e: public entry point, host camera in, pinned host image out ----
     img_bytes = WIDTH * HEIGHT * 8
     pinned = torch.empty(img_bytes * 2, dtype=torch.uint8, pin_memory=True)
-    e2e_views = min(len(cam_structs), 32)
     for _ in range(2):
         check(lib.gs3d_rebin(ctx, C.byref(cam_structs[0]), WIDTH, HEIGHT))
     check(lib.gs3d_synchronize(ctx))
@@ -221,7 +219,7 @@ def run_ours(args, rank, world):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for k in range(args.steps):
-        for v in range(e2e_views):
+        for v in range(len(cams)):
             cs = camera_struct(cams[v])  # host struct built per view
             check(lib.gs3d_rebin(ctx, C.byref(cs), WIDTH, HEIGHT))
             check(lib.gs3d_copy_buffer_async(ctx, 14, C.c_void_p(pinned.data_ptr() +
@@ -230,33 +228,36 @@ def run_ours(args, rank, world):
     check(lib.gs3d_synchronize(ctx))
     e2e_wall = time.perf_counter() - t0
     e2e_ms = e0.elapsed_time(e1)
-    e2e_views_total = args.steps * e2e_views
-
     lib.gs3d_destroy(ctx)
 
-    # ---- roofline of the dominant HBM-bound kernel ----
     tiles = (WIDTH // TILE) * -(-HEIGHT // TILE)
-    tile_bits = (tiles - 1).bit_length()
-    plan_passes = 4 + (tile_bits + 7) // 8  # depth digits + non-zero tile-id digits
+    tile_passes = ((tiles - 1).bit_length() + 7) // 8
     mean_R = float(np.mean(refs))
-    algo = algorithmic_bytes(N_SPLATS, mean_R, tiles, plan_passes, 45)
     peak, peak_kind = peaks()
-    per_stage = {}
-    for s, name in enumerate(STAGES):
-        gbs = algo[name] / (stage_ms[s] * 1e-3) / 1e9
-        per_stage[name] = {"ms": round(float(stage_ms[s]), 4), "algo_bytes": int(algo[name]),
-                           "gbs": round(gbs, 1), "frac_hbm": round(gbs / peak, 3)}
-    hbm_stages = [s for s in STAGES if s != "rasterize-tiles"]
-    dom = max(hbm_stages, key=lambda s: per_stage[s]["ms"])
-    value = views * world / (total_ms * 1e-3)  # weak scaling: every rank renders its views
+
+    def roof(stages, fused):
+        algo = algorithmic_bytes(N_SPLATS, mean_R, tiles, tile_passes, 45, fused)
+        out = {}
+        for name, (ms, n) in stages.items():
+            gbs = algo[name] / (ms * 1e-3) / 1e9
+            out[name] = {"ms": round(ms, 4), "algo_bytes": int(algo[name]), "gbs": round(gbs, 1),
+                         "frac_hbm": round(gbs / peak, 3)}
+        return out
+
+    fused_roof = roof(fused_stages, True)
+    hbm = [s for s in fused_roof if s != "rasterize-tiles"]
+    dom = max(hbm, key=lambda s: fused_roof[s]["ms"])
+    launches = 1 + 5 + 1 + 1 + tile_passes + 1 + 1  # preprocess, depth sort, scan, emit, ...
     return {
-        "value": value, "ms_per_step": total_ms / args.steps, "views": views,
-        "per_stage": per_stage, "dominant": dom, "peak": peak, "peak_kind": peak_kind,
-        "mean_refs": mean_R, "passes": plan_passes, "clocks": clocks.summary(),
-        "e2e_value": e2e_views_total * world / (e2e_ms * 1e-3),
-        "e2e_wall_value": e2e_views_total / e2e_wall,
+        "value": views * world / (fused_ms * 1e-3), "ms_per_step": fused_ms / args.steps,
+        "views": views, "per_stage": fused_roof, "dominant": dom, "peak": peak,
+        "peak_kind": peak_kind, "mean_refs": mean_R, "tile_passes": tile_passes,
+        "clocks": clocks,
+        "stagewise_value": views * world / (stagewise_ms * 1e-3),
+        "stagewise_stages": roof(stagewise_stages, False),
+        "e2e_value": views * world / (e2e_ms * 1e-3), "e2e_wall_value": views / e2e_wall,
         "h2d": 288 * len(cam_structs), "d2h": img_bytes * len(cam_structs),
-        "launches_per_view": 5 + plan_passes + 1,
+        "launches_per_view": launches,
     }
 
 
@@ -324,13 +325,16 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "path": "plain single-view",
+            "config": {"workload": WORKLOAD, "path": "single-view fused rebin",
                        "views_per_step": args.views, "l2": "inputs larger than L2 (no flush)",
-                       "mean_refs_per_view": res["mean_refs"], "sort_passes": res["passes"]},
+                       "mean_refs_per_view": res["mean_refs"],
+                       "tile_digit_passes": res["tile_passes"],
+                       "stagewise_views_per_s": res["stagewise_value"]},
             "roofline": {"bound": "hbm", "kernel": res["dominant"], "achieved": dom["gbs"],
                          "peak": res["peak"], "unit": "GB/s", "frac": dom["frac_hbm"],
                          "peak_kind": res["peak_kind"], "traffic": None},
             "stages": res["per_stage"],
+            "stages_stagewise": res["stagewise_stages"],
             "cpu_baseline": cpu,
             "e2e": {"value": res["e2e_value"], "unit": "views/s",
                     "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],

@@ -77,8 +77,31 @@ typedef struct gs3d_config {
                                      truncated.                                    */
     void*    stream;              /* cudaStream_t to enqueue on; NULL -> the
                                      library creates a non-blocking stream         */
-    uint32_t flags;               /* reserved, 0                                   */
+    uint32_t flags;               /* GS3D_FLAG_* bits                              */
 } gs3d_config;
+
+/* gs3d_rebin runs the fused path by default: the four depth-digit passes of
+ * the LSD sort are applied to the N splats before their refs are expanded
+ * (every ref of a splat shares its depth), refs are emitted in depth order
+ * and only the tile-id digits are sorted over the R refs.  The result (sorted
+ * keys, values, tile_offsets, image) is identical to the stage-wise path; the
+ * stage-wise path additionally leaves splat_ref_offsets in splat order.  This
+ * flag selects the stage-wise path (the six reference stages in order). */
+#define GS3D_FLAG_STAGEWISE_REBIN 1u
+/* Records a CUDA event pair around every stage on the context's stream;
+ * gs3d_read_stage_times returns the accumulated device time per stage. */
+#define GS3D_FLAG_STAGE_TIMING    2u
+
+/* Stage indices of gs3d_read_stage_times (the reference's profiler labels,
+ * GaussianSplatRenderer.ts:1144-1260, plus the fused path's depth sort). */
+#define GS3D_STAGE_PREPROCESS 0  /* preprocess-splats                         */
+#define GS3D_STAGE_DEPTH_SORT 1  /* fused path: per-splat depth digits        */
+#define GS3D_STAGE_SCAN       2  /* prefix-scan-*                             */
+#define GS3D_STAGE_EMIT       3  /* emit-tile-refs                            */
+#define GS3D_STAGE_SORT       4  /* radix-* (fused path: tile digits only)    */
+#define GS3D_STAGE_IDENTIFY   5  /* identify-tile-ranges                      */
+#define GS3D_STAGE_RASTER     6  /* rasterize-tiles                           */
+#define GS3D_STAGE_COUNT      7
 
 /* Named device buffers (BufferManager names, GaussianSplatRenderer.ts:338-465). */
 typedef enum gs3d_buffer {
@@ -149,6 +172,14 @@ int gs3d_rasterize_tiles(struct gs3d_ctx* ctx);     /* rasterize_tiles.wgsl     
 /* rebin (GaussianSplatRenderer.ts:1104-1266): set_camera + all six stages. */
 int gs3d_rebin(struct gs3d_ctx* ctx, const gs3d_camera* cam,
                uint32_t width, uint32_t height);
+
+/* Replaces the context's GS3D_FLAG_* bits. */
+int gs3d_set_flags(struct gs3d_ctx* ctx, uint32_t flags);
+
+/* With GS3D_FLAG_STAGE_TIMING: waits for the recorded stages, writes the
+ * device milliseconds and stage executions accumulated since the last call
+ * (GS3D_STAGE_COUNT entries each; either pointer may be NULL) and resets. */
+int gs3d_read_stage_times(struct gs3d_ctx* ctx, double* ms, uint32_t* executions);
 
 /* Waits for the context's stream and reports latched device errors.  After
  * GS3D_ERR_CAPACITY the key buffers have already been grown to the observed

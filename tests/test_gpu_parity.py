@@ -34,16 +34,18 @@ def oracle_frame(oracle, data, uniform, w, h, tw, th):
                         data.colors, data.sphericalHarmonics, data.sphericalHarmonicsDegree)
 
 
-def gpu_frame(r, data, uniform, w, h, tw=16, th=16):
+def gpu_frame(r, data, uniform, w, h, tw=16, th=16, stagewise=False):
     r.setTileSize(tw, th)
     r.setSplatData(data)
+    r.setStagewise(stagewise)
     tx, ty = -(-w // tw), -(-h // th)
     r.rebin(data.splatCount, tx, ty, w, h, uniform)
+    r.setStagewise(False)
     R = r.refCount()
     return dict(
         projected_splats=r.readBuffer("projected_splats"),
         splat_ref_counts=r.readBuffer("splat_ref_counts"),
-        splat_ref_offsets=r.readBuffer("splat_ref_offsets"),
+        splat_ref_offsets=r.readBuffer("splat_ref_offsets") if stagewise else None,
         ref_counter=R,
         sort_keys_a=r.readBuffer("sort_keys_a", R),
         sort_values_a=r.readBuffer("sort_values_a", R),
@@ -70,7 +72,8 @@ def assert_frame_match(g, o, exact_preprocess=True):
     if exact_preprocess:
         assert g["projected_splats"].tobytes() == o["projected_splats"].tobytes()
     assert np.array_equal(g["splat_ref_counts"], o["splat_ref_counts"])
-    assert np.array_equal(g["splat_ref_offsets"], o["splat_ref_offsets"])
+    if g["splat_ref_offsets"] is not None:  # stage-wise path: reference splat order
+        assert np.array_equal(g["splat_ref_offsets"], o["splat_ref_offsets"])
     assert g["ref_counter"] == o["ref_counter"]
     assert np.array_equal(g["sort_keys_a"], o["sort_keys_a"])
     assert np.array_equal(g["sort_values_a"], o["sort_values_a"])
@@ -83,12 +86,14 @@ def assert_frame_match(g, o, exact_preprocess=True):
     assert np.abs(gc - oc).sum() <= 0.01 * max(1, oc.sum())
 
 
-def test_small_scene_end_to_end(renderer, oracle):
-    """The small benchmark scene: 100k splats, SH 0, 1280x720, 16x16 tiles."""
+@pytest.mark.parametrize("stagewise", [False, True])
+def test_small_scene_end_to_end(renderer, oracle, stagewise):
+    """The small benchmark scene: 100k splats, SH 0, 1280x720, 16x16 tiles,
+    through the fused rebin and through the six reference stages."""
     data = scenes.scene_small(100_000, seed=0)
     u = scenes.small_camera().getUniformData(1280, 720)
     o = oracle_frame(oracle, data, u, 1280, 720, 16, 16)
-    g = gpu_frame(renderer, data, u, 1280, 720)
+    g = gpu_frame(renderer, data, u, 1280, 720, stagewise=stagewise)
     assert o["ref_counter"] > 100_000
     assert_frame_match(g, o)
 
@@ -103,29 +108,32 @@ def test_sh_colour_degrees(renderer, oracle, deg):
 
 
 @pytest.mark.parametrize("w,h,tw,th", [(1000, 563, 16, 16), (640, 360, 8, 8), (1024, 600, 32, 32),
-                                       (333, 217, 12, 20), (17, 9, 16, 16)])
-def test_ragged_viewports_and_tile_sizes(renderer, oracle, w, h, tw, th):
+                                       (333, 217, 12, 20), (17, 9, 16, 16), (4000, 40, 4, 4)])
+@pytest.mark.parametrize("stagewise", [False, True])
+def test_ragged_viewports_and_tile_sizes(renderer, oracle, w, h, tw, th, stagewise):
     data = scenes.scene_small(40_000, seed=5)
     u = scenes.small_camera(w, h).getUniformData(w, h)
     o = oracle_frame(oracle, data, u, w, h, tw, th)
-    g = gpu_frame(renderer, data, u, w, h, tw, th)
+    g = gpu_frame(renderer, data, u, w, h, tw, th, stagewise=stagewise)
     assert_frame_match(g, o)
     renderer.setTileSize(16, 16)
 
 
-def test_empty_scene(renderer):
+@pytest.mark.parametrize("stagewise", [False, True])
+def test_empty_scene(renderer, stagewise):
     z = np.zeros((0, 4), np.float32)
     data = scenes.GaussianSplatData(z, z, z, z, None, 0, 0)
     u = scenes.small_camera(320, 200).getUniformData(320, 200)
-    g = gpu_frame(renderer, data, u, 320, 200)
+    g = gpu_frame(renderer, data, u, 320, 200, stagewise=stagewise)
     assert g["ref_counter"] == 0
     assert not g["tile_offsets"].any() and not g["image"].any()
 
 
-def test_everything_culled(renderer):
+@pytest.mark.parametrize("stagewise", [False, True])
+def test_everything_culled(renderer, stagewise):
     data = scenes.scene_small(10_000, seed=1)
     u = scenes.camera_at((0, 0, 30), 320, 200, target=(0, 0, 60)).getUniformData(320, 200)
-    g = gpu_frame(renderer, data, u, 320, 200)
+    g = gpu_frame(renderer, data, u, 320, 200, stagewise=stagewise)
     assert g["ref_counter"] == 0 and not g["projected_splats"]["valid"].any()
     assert not g["image"].any()
 
@@ -249,3 +257,41 @@ def test_errors_are_status_codes(renderer):
     with pytest.raises(Gs3dError) as ei:
         renderer._call("gs3d_set_splats", 1, None, None, None, None, None, 0, 0)
     assert ei.value.code == _lib.ERR_INVALID_ARG
+
+
+def test_fused_equals_stagewise_at_full_size(renderer):
+    """The 3M-splat SH-3 1080p workload: the fused rebin and the six-stage
+    rebin give bit-identical sorted keys, values, tile ranges and images, and
+    the result satisfies the size-independent properties of a correct sort."""
+    data = scenes.scene_clusters(3_000_000, seed=0, sh_degree=3)
+    w, h = 1920, 1080
+    u = scenes.camera_at(scenes.orbit_eyes(64)[5], w, h).getUniformData(w, h)
+    out = []
+    for sw in (False, True):
+        renderer.setTileSize(16, 16)
+        renderer.setSplatData(data)
+        renderer.setStagewise(sw)
+        renderer.rebin(data.splatCount, 120, 68, w, h, u)
+        R = renderer.refCount()
+        out.append((R, renderer.readBuffer("sort_keys_a", R), renderer.readBuffer("sort_values_a", R),
+                    renderer.readBuffer("tile_offsets"), renderer.readImage(),
+                    renderer.readBuffer("splat_ref_counts"), renderer.readBuffer("projected_splats")))
+    renderer.setStagewise(False)
+    (R, k, v, t, img, cnt, proj), (R2, k2, v2, t2, img2, _, _) = out
+    assert R == R2 and R == int(cnt.astype(np.int64).sum()) and R > 10_000_000
+    assert np.array_equal(k, k2) and np.array_equal(v, v2)
+    assert np.array_equal(t, t2) and np.array_equal(img.view(np.uint16), img2.view(np.uint16))
+    # sortedness: (tile, depth bits, splat id) strictly increasing
+    key64 = (k[:, 0].astype(np.uint64) << np.uint64(32)) | k[:, 1].astype(np.uint64)
+    d = np.diff(key64.astype(np.float64))  # exactness not needed for the sign test below
+    same = key64[1:] == key64[:-1]
+    assert np.all((key64[1:] > key64[:-1]) | (same & (v[1:] > v[:-1])))
+    # every ref names a valid splat whose depth bits and tile rectangle match
+    assert np.all(proj["valid"][v] == 1)
+    assert np.array_equal(k[:, 1], (-proj["depth"][v]).view(np.uint32))
+    tx, ty = k[:, 0] % 120, k[:, 0] // 120
+    assert np.all((proj["tile_min"][v, 0] <= tx) & (tx <= proj["tile_max"][v, 0]))
+    assert np.all((proj["tile_min"][v, 1] <= ty) & (ty <= proj["tile_max"][v, 1]))
+    # per-splat ref multiplicity equals its count
+    assert np.array_equal(np.bincount(v, minlength=len(cnt)), cnt)
+    del d

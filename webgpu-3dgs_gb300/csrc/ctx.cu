@@ -22,6 +22,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "gs3d_internal.cuh"
 
@@ -52,6 +53,7 @@ struct gs3d_ctx {
   std::string err = "no error";
 
   uint32_t tile_w = 16, tile_h = 16, max_tiles_per_splat = 16;
+  uint32_t flags = 0;
 
   // scene (SceneSyncer buffers)
   bool have_scene = false;
@@ -64,6 +66,8 @@ struct gs3d_ctx {
   uint32_t capacity = 0;
   DevBuf scan_status, sort_status;
   uint32_t scan_epoch = 0;
+  // fused rebin: per-splat depth keys/ids (ping-pong), offsets in depth order
+  DevBuf depth_keys_a, depth_ids_a, depth_keys_b, depth_ids_b, sorted_offsets, depth_status;
 
   // frame
   bool have_camera = false;
@@ -76,6 +80,17 @@ struct gs3d_ctx {
 
   DevBuf ctrl;
   uint32_t* h_word = nullptr;  // pinned scratch for small reads
+
+  // optional stage timing (GS3D_FLAG_STAGE_TIMING)
+  struct Pending {
+    int stage;
+    cudaEvent_t a, b;
+  };
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_next = 0;
+  std::vector<Pending> pending;
+  double stage_ms[GS3D_STAGE_COUNT] = {};
+  uint32_t stage_n[GS3D_STAGE_COUNT] = {};
 };
 
 namespace {
@@ -192,6 +207,44 @@ int check_device_errors(gs3d_ctx* c) {
               "a sort key's tile id or a splat offset was out of range for this frame");
 }
 
+constexpr size_t kEventPool = 4096;
+
+int drain_timing(gs3d_ctx* c) {
+  for (const auto& p : c->pending) {
+    CK(cudaEventSynchronize(p.b), "stage timing");
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, p.a, p.b), "stage timing");
+    c->stage_ms[p.stage] += ms;
+    c->stage_n[p.stage] += 1;
+  }
+  c->pending.clear();
+  c->ev_next = 0;
+  return GS3D_OK;
+}
+
+// RAII pair of events around one stage when timing is on.
+struct StageScope {
+  gs3d_ctx* c;
+  int stage;
+  cudaEvent_t a = nullptr;
+  StageScope(gs3d_ctx* ctx, int st) : c(ctx), stage(st) {
+    if (!(c->flags & GS3D_FLAG_STAGE_TIMING)) return;
+    if (c->ev_pool.empty()) {
+      c->ev_pool.resize(kEventPool);
+      for (auto& e : c->ev_pool) cudaEventCreate(&e);
+    }
+    if (c->ev_next + 2 > c->ev_pool.size()) drain_timing(c);
+    a = c->ev_pool[c->ev_next++];
+    cudaEventRecord(a, c->stream);
+  }
+  ~StageScope() {
+    if (!a) return;
+    cudaEvent_t b = c->ev_pool[c->ev_next++];
+    cudaEventRecord(b, c->stream);
+    c->pending.push_back({stage, a, b});
+  }
+};
+
 int sync_and_check(gs3d_ctx* c) {
   CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
   return check_device_errors(c);
@@ -218,6 +271,7 @@ int gs3d_create(gs3d_ctx** out, const gs3d_config* cfg) {
   if (cfg->tile_w) c->tile_w = cfg->tile_w;
   if (cfg->tile_h) c->tile_h = cfg->tile_h;
   if (cfg->max_tiles_per_splat) c->max_tiles_per_splat = cfg->max_tiles_per_splat;
+  c->flags = cfg->flags;
   auto bail = [&](int rc) {
     gs3d_destroy(c);
     return rc;
@@ -272,10 +326,13 @@ int gs3d_destroy(gs3d_ctx* c) {
                     &c->sh,         &c->proj,         &c->counts,      &c->offsets,
                     &c->ref_counter, &c->keys_a,      &c->vals_a,      &c->keys_b,
                     &c->vals_b,     &c->scan_status,  &c->sort_status, &c->frame,
-                    &c->tile_offsets, &c->image,      &c->tile_costs,  &c->ctrl};
+                    &c->tile_offsets, &c->image,      &c->tile_costs,  &c->ctrl,
+                    &c->depth_keys_a, &c->depth_ids_a, &c->depth_keys_b, &c->depth_ids_b,
+                    &c->sorted_offsets, &c->depth_status};
   for (DevBuf* b : bufs) release(*b);
   for (int i = 0; i < kFrameSlots; ++i)
     if (c->frame_ev[i]) cudaEventDestroy(c->frame_ev[i]);
+  for (auto& e : c->ev_pool) cudaEventDestroy(e);
   if (c->h_frames) cudaFreeHost(c->h_frames);
   if (c->h_word) cudaFreeHost(c->h_word);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -317,6 +374,12 @@ int gs3d_set_splats(gs3d_ctx* c, uint32_t n, const float* positions, const float
   TRY(ensure(c, c->counts, (size_t)n * 4, "splat_ref_counts"));
   TRY(ensure(c, c->offsets, ((size_t)n + 1) * 4, "splat_ref_offsets"));
   TRY(ensure(c, c->scan_status, scan_status_words(n) * 8, "scan look-back status"));
+  TRY(ensure(c, c->depth_keys_a, (size_t)n * 4, "depth keys"));
+  TRY(ensure(c, c->depth_keys_b, (size_t)n * 4, "depth keys"));
+  TRY(ensure(c, c->depth_ids_a, (size_t)n * 4, "depth ids"));
+  TRY(ensure(c, c->depth_ids_b, (size_t)n * 4, "depth ids"));
+  TRY(ensure(c, c->sorted_offsets, ((size_t)n + 1) * 4, "depth-ordered offsets"));
+  TRY(ensure(c, c->depth_status, sort_status_words(n, 4) * 4, "depth sort status"));
   TRY(ensure_key_capacity(
       c, std::min<uint64_t>((uint64_t)std::max<uint32_t>(n, 1) * c->max_tiles_per_splat,
                             kMaxCapacity)));
@@ -388,13 +451,82 @@ int gs3d_preprocess(gs3d_ctx* c) {
   TRY(set_device(c));
   // start of a frame: counters, histograms and the error latch
   CK(cudaMemsetAsync(c->ctrl.p, 0, sizeof(Ctrl), c->stream), "reset control block");
+  StageScope t(c, GS3D_STAGE_PREPROCESS);
   CK(launch_preprocess(static_cast<FrameUniforms*>(c->frame.p), c->n,
                        static_cast<float4*>(c->pos.p), static_cast<float4*>(c->scale.p),
                        static_cast<float4*>(c->rot.p), static_cast<float4*>(c->color.p),
                        c->sh_degree ? static_cast<float*>(c->sh.p) : nullptr, c->sh_degree,
                        static_cast<gs3d_projected_splat*>(c->proj.p),
-                       static_cast<uint32_t*>(c->counts.p), &ctrl_of(c)->error, c->stream),
+                       static_cast<uint32_t*>(c->counts.p), nullptr, nullptr,
+                       &ctrl_of(c)->error, c->stream),
      "preprocess");
+  return GS3D_OK;
+}
+
+// Fused rebin (the default): depth digits sorted over splats, refs emitted in
+// depth order, tile digits sorted over refs.  Same sorted keys, values,
+// tile_offsets and image as the stage-wise sequence.
+static int fused_rebin(gs3d_ctx* c) {
+  TRY(require_frame(c, "rebin"));
+  Ctrl* k = ctrl_of(c);
+  FrameUniforms* fu = static_cast<FrameUniforms*>(c->frame.p);
+  CK(cudaMemsetAsync(c->ctrl.p, 0, sizeof(Ctrl), c->stream), "reset control block");
+  auto u32 = [](DevBuf& b) { return static_cast<uint32_t*>(b.p); };
+  {
+  StageScope t(c, GS3D_STAGE_PREPROCESS);
+  CK(launch_preprocess(fu, c->n, static_cast<float4*>(c->pos.p), static_cast<float4*>(c->scale.p),
+                       static_cast<float4*>(c->rot.p), static_cast<float4*>(c->color.p),
+                       c->sh_degree ? static_cast<float*>(c->sh.p) : nullptr, c->sh_degree,
+                       static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->counts),
+                       u32(c->depth_keys_a), u32(c->depth_ids_a), &k->error, c->stream),
+     "preprocess");
+  }
+  {
+  StageScope t(c, GS3D_STAGE_DEPTH_SORT);
+  CK(launch_sort_depth_keys(&fu->splat_count, c->n, u32(c->depth_keys_a), u32(c->depth_ids_a),
+                            u32(c->depth_keys_b), u32(c->depth_ids_b), u32(c->depth_status),
+                            &k->sort_hist[0][0], &k->sort_part_counter[0], &k->error,
+                            c->sm_count, c->stream),
+     "depth sort");
+  }
+  c->scan_epoch = (c->scan_epoch % ((1u << 30) - 1)) + 1;
+  {
+  StageScope t(c, GS3D_STAGE_SCAN);
+  CK(launch_scan(u32(c->counts), u32(c->depth_ids_a), u32(c->sorted_offsets), c->n,
+                 static_cast<unsigned long long*>(c->scan_status.p), &k->scan_tile_counter,
+                 c->scan_epoch, u32(c->ref_counter), &k->error, c->stream),
+     "prefix scan (depth order)");
+  }
+  const SortPlan full = make_sort_plan(c->tiles_x * c->tiles_y);
+  SortPlan tp{};
+  for (int p = 4; p < full.passes; ++p) {  // the tile-id digit places only
+    tp.word[tp.passes] = full.word[p];
+    tp.shift[tp.passes] = full.shift[p];
+    ++tp.passes;
+  }
+  {
+  StageScope t(c, GS3D_STAGE_EMIT);
+  CK(launch_emit_sorted(fu, c->n, static_cast<gs3d_projected_splat*>(c->proj.p),
+                        u32(c->depth_ids_a), u32(c->sorted_offsets), u32(c->ref_counter),
+                        c->capacity, static_cast<uint2*>(c->keys_a.p), u32(c->vals_a), tp,
+                        &k->sort_hist[4][0], &k->error, c->stream),
+     "emit (depth order)");
+  }
+  {
+  StageScope t(c, GS3D_STAGE_SORT);
+  CK(launch_sort_tile_passes(tp, u32(c->ref_counter), c->capacity,
+                             static_cast<uint2*>(c->keys_a.p), u32(c->vals_a),
+                             static_cast<uint2*>(c->keys_b.p), u32(c->vals_b),
+                             u32(c->sort_status), &k->sort_hist[4][0], &k->sort_part_counter[4],
+                             &k->error, c->sm_count, c->stream),
+     "tile-digit sort");
+  }
+  if (tp.passes % 2) {
+    std::swap(c->keys_a, c->keys_b);
+    std::swap(c->vals_a, c->vals_b);
+  }
+  TRY(gs3d_identify_tile_ranges(c));
+  TRY(gs3d_rasterize_tiles(c));
   return GS3D_OK;
 }
 
@@ -405,7 +537,9 @@ int gs3d_prefix_scan(gs3d_ctx* c) {
   CK(cudaMemsetAsync(&ctrl_of(c)->scan_tile_counter, 0, sizeof(uint32_t), c->stream),
      "reset scan ticket");
   c->scan_epoch = (c->scan_epoch % ((1u << 30) - 1)) + 1;  // 1 .. 2^30-1, never 0
-  CK(launch_scan(static_cast<uint32_t*>(c->counts.p), static_cast<uint32_t*>(c->offsets.p), c->n,
+  StageScope t(c, GS3D_STAGE_SCAN);
+  CK(launch_scan(static_cast<uint32_t*>(c->counts.p), nullptr,
+                 static_cast<uint32_t*>(c->offsets.p), c->n,
                  static_cast<unsigned long long*>(c->scan_status.p),
                  &ctrl_of(c)->scan_tile_counter, c->scan_epoch,
                  static_cast<uint32_t*>(c->ref_counter.p), &ctrl_of(c)->error, c->stream),
@@ -417,6 +551,7 @@ int gs3d_emit_tile_refs(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
   TRY(require_frame(c, "emit_tile_refs"));
   TRY(set_device(c));
+  StageScope t(c, GS3D_STAGE_EMIT);
   CK(launch_emit(static_cast<FrameUniforms*>(c->frame.p), c->n,
                  static_cast<gs3d_projected_splat*>(c->proj.p),
                  static_cast<uint32_t*>(c->offsets.p), static_cast<uint32_t*>(c->ref_counter.p),
@@ -431,11 +566,14 @@ int gs3d_radix_sort(gs3d_ctx* c) {
   TRY(require_frame(c, "radix_sort"));
   TRY(set_device(c));
   const SortPlan plan = make_sort_plan(c->tiles_x * c->tiles_y);
+  {
+  StageScope t(c, GS3D_STAGE_SORT);
   CK(launch_sort(plan, static_cast<uint32_t*>(c->ref_counter.p), c->capacity,
                  static_cast<uint2*>(c->keys_a.p), static_cast<uint32_t*>(c->vals_a.p),
                  static_cast<uint2*>(c->keys_b.p), static_cast<uint32_t*>(c->vals_b.p),
                  static_cast<uint32_t*>(c->sort_status.p), ctrl_of(c), c->sm_count, c->stream),
      "radix sort");
+  }
   if (plan.passes % 2) {  // sorted data ended in the B buffers: rename
     std::swap(c->keys_a, c->keys_b);
     std::swap(c->vals_a, c->vals_b);
@@ -447,6 +585,7 @@ int gs3d_identify_tile_ranges(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
   TRY(require_frame(c, "identify_tile_ranges"));
   TRY(set_device(c));
+  StageScope t(c, GS3D_STAGE_IDENTIFY);
   CK(launch_identify(static_cast<uint2*>(c->keys_a.p), static_cast<uint32_t*>(c->ref_counter.p),
                      c->capacity, c->tiles_x * c->tiles_y,
                      static_cast<uint32_t*>(c->tile_offsets.p), &ctrl_of(c)->error, c->sm_count,
@@ -459,6 +598,7 @@ int gs3d_rasterize_tiles(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
   TRY(require_frame(c, "rasterize_tiles"));
   TRY(set_device(c));
+  StageScope t(c, GS3D_STAGE_RASTER);
   CK(launch_raster(static_cast<FrameUniforms*>(c->frame.p), c->tiles_x, c->tiles_y, c->tile_w,
                    c->tile_h, static_cast<gs3d_projected_splat*>(c->proj.p),
                    static_cast<uint32_t*>(c->tile_offsets.p),
@@ -471,12 +611,35 @@ int gs3d_rasterize_tiles(gs3d_ctx* c) {
 int gs3d_rebin(gs3d_ctx* c, const gs3d_camera* cam, uint32_t width, uint32_t height) {
   if (!c) return GS3D_ERR_INVALID_ARG;
   TRY(gs3d_set_camera(c, cam, width, height));
+  TRY(set_device(c));
+  if (!(c->flags & GS3D_FLAG_STAGEWISE_REBIN)) return fused_rebin(c);
   TRY(gs3d_preprocess(c));
   TRY(gs3d_prefix_scan(c));
   TRY(gs3d_emit_tile_refs(c));
   TRY(gs3d_radix_sort(c));
   TRY(gs3d_identify_tile_ranges(c));
   TRY(gs3d_rasterize_tiles(c));
+  return GS3D_OK;
+}
+
+int gs3d_read_stage_times(gs3d_ctx* c, double* ms, uint32_t* n) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  TRY(set_device(c));
+  TRY(drain_timing(c));
+  for (int i = 0; i < GS3D_STAGE_COUNT; ++i) {
+    if (ms) ms[i] = c->stage_ms[i];
+    if (n) n[i] = c->stage_n[i];
+    c->stage_ms[i] = 0.0;
+    c->stage_n[i] = 0;
+  }
+  return GS3D_OK;
+}
+
+int gs3d_set_flags(gs3d_ctx* c, uint32_t flags) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  if (flags & ~(GS3D_FLAG_STAGEWISE_REBIN | GS3D_FLAG_STAGE_TIMING))
+    return fail(c, GS3D_ERR_INVALID_ARG, "unknown flag bits 0x%x", flags);
+  c->flags = flags;
   return GS3D_OK;
 }
 

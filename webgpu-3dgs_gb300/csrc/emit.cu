@@ -79,7 +79,120 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Fused-rebin emit: block b owns depth-sorted positions [256b, 256b+256); the
+// splat at position i is sorted_ids[i] and its refs start at
+// sorted_offsets[i].  Besides the keys/values it accumulates the 256-bin
+// histograms of the tile-id digit places that the following radix passes
+// sort, so those passes need no separate histogram read.
+template <int TP>
+__global__ void __launch_bounds__(kThreads)
+    emit_sorted_kernel(const FrameUniforms* __restrict__ fu, uint32_t n,
+                       const gs3d_projected_splat* __restrict__ proj,
+                       const uint32_t* __restrict__ sorted_ids,
+                       const uint32_t* __restrict__ sorted_offsets,
+                       const uint32_t* __restrict__ ref_counter, uint32_t capacity,
+                       uint2* __restrict__ keys, uint32_t* __restrict__ values, int4 shifts,
+                       uint32_t* __restrict__ g_hist, uint32_t* __restrict__ err) {
+  __shared__ uint32_t s_off[kThreads + 1];
+  __shared__ uint32_t s_tminx[kThreads], s_tminy[kThreads], s_w[kThreads], s_cnt[kThreads];
+  __shared__ uint32_t s_lo[kThreads], s_id[kThreads];
+  __shared__ uint32_t s_hist[TP > 0 ? TP : 1][kRadixBins];
+
+  const uint32_t total = *ref_counter;
+  if (total > capacity) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) latch_error(err, DEVERR_CAPACITY);
+    return;
+  }
+  for (int k = threadIdx.x; k < TP * kRadixBins; k += kThreads) (&s_hist[0][0])[k] = 0u;
+  const uint32_t first = blockIdx.x * kThreads;
+  const uint32_t i = first + threadIdx.x;
+  const uint32_t tiles_x = __ldg(&fu->tile_count[0]);
+  if (i < n) {
+    const uint32_t id = __ldg(sorted_ids + i);
+    const float4 r0 = __ldg(reinterpret_cast<const float4*>(proj + id));
+    const uint32_t valid = __ldg(&proj[id].valid);
+    const uint4 r3 = __ldg(reinterpret_cast<const uint4*>(proj + id) + 3);
+    const uint32_t w = r3.z - r3.x + 1u, h = r3.w - r3.y + 1u;
+    s_off[threadIdx.x] = __ldg(sorted_offsets + i);
+    s_tminx[threadIdx.x] = r3.x;
+    s_tminy[threadIdx.x] = r3.y;
+    s_w[threadIdx.x] = w;
+    s_cnt[threadIdx.x] = valid ? w * h : 0u;
+    s_lo[threadIdx.x] = __float_as_uint(-r0.z);
+    s_id[threadIdx.x] = id;
+  }
+  const uint32_t last = min(n, first + kThreads);
+  if (threadIdx.x == 0) s_off[last - first] = __ldg(sorted_offsets + last);
+  __syncthreads();
+
+  const uint32_t nloc = last - first;
+  const uint32_t begin = s_off[0], end = s_off[nloc];
+  if (end < begin || end > total) {
+    if (threadIdx.x == 0) latch_error(err, DEVERR_RANGE);
+    return;
+  }
+  const int sh[4] = {shifts.x, shifts.y, shifts.z, shifts.w};
+  for (uint32_t base = begin; base < end; base += kThreads) {  // warp-uniform trip count
+    const uint32_t j = base + threadIdx.x;
+    bool live = j < end;
+    uint32_t tile = 0;
+    if (live) {
+      uint32_t lo = 0, hi = nloc;
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (s_off[mid] <= j) lo = mid; else hi = mid;
+      }
+      const uint32_t k = j - s_off[lo];
+      if (k < s_cnt[lo]) {
+        const uint32_t w = s_w[lo];
+        tile = (s_tminy[lo] + k / w) * tiles_x + s_tminx[lo] + k % w;
+        keys[j] = make_uint2(tile, s_lo[lo]);
+        values[j] = s_id[lo];
+      } else {
+        live = false;
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < TP; ++p) hist_add_256(s_hist[p], (tile >> sh[p]) & 0xffu, live);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < TP * kRadixBins; k += kThreads) {
+    const uint32_t v = (&s_hist[0][0])[k];
+    if (v) atomicAdd(g_hist + k, v);
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_emit_sorted(const FrameUniforms* d_frame, uint32_t n,
+                               const gs3d_projected_splat* proj, const uint32_t* sorted_ids,
+                               const uint32_t* sorted_offsets, const uint32_t* ref_counter,
+                               uint32_t capacity, uint2* keys, uint32_t* values,
+                               const SortPlan& tile_plan, uint32_t* g_hist, uint32_t* err,
+                               cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  const uint32_t blocks = (n + kThreads - 1) / kThreads;
+  int4 sh = make_int4(0, 0, 0, 0);
+  int* shp = &sh.x;
+  for (int p = 0; p < tile_plan.passes && p < 4; ++p) shp[p] = tile_plan.shift[p];
+#define GS3D_EMIT_CASE(TP)                                                                   \
+  case TP:                                                                                  \
+    emit_sorted_kernel<TP><<<blocks, kThreads, 0, s>>>(d_frame, n, proj, sorted_ids,         \
+                                                       sorted_offsets, ref_counter, capacity, \
+                                                       keys, values, sh, g_hist, err);        \
+    break;
+  switch (tile_plan.passes) {
+    GS3D_EMIT_CASE(0)
+    GS3D_EMIT_CASE(1)
+    GS3D_EMIT_CASE(2)
+    GS3D_EMIT_CASE(3)
+    GS3D_EMIT_CASE(4)
+    default:
+      return cudaErrorInvalidValue;
+  }
+#undef GS3D_EMIT_CASE
+  return cudaGetLastError();
+}
 
 cudaError_t launch_emit(const FrameUniforms* d_frame, uint32_t n,
                         const gs3d_projected_splat* proj, const uint32_t* offsets,

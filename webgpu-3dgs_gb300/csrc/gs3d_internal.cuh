@@ -129,6 +129,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 
 __device__ __forceinline__ void latch_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }
 
+// Shared-memory histogram add with a warp-uniform fast path: coherent digits
+// (the high byte of neighbouring tile ids, a depth exponent byte) would
+// otherwise serialise the lanes of a warp on one address.  Every lane of the
+// warp must call it.
+__device__ __forceinline__ void hist_add_256(uint32_t* h, uint32_t d, bool active) {
+  const uint32_t act = __ballot_sync(0xffffffffu, active);
+  const uint32_t d0 = __shfl_sync(0xffffffffu, d, act ? __ffs(act) - 1 : 0);
+  const bool same = __all_sync(0xffffffffu, !active || d == d0);
+  if (same) {
+    if (act && (threadIdx.x & 31) == (uint32_t)(__ffs(act) - 1)) atomicAdd(h + d0, __popc(act));
+  } else if (active) {
+    atomicAdd(h + d, 1u);
+  }
+}
+
 // Live ref count guarded by capacity: a count above capacity was latched as
 // DEVERR_CAPACITY by emit and every later stage treats it as zero.
 __device__ __forceinline__ uint32_t live_refs(const uint32_t* ref_counter, uint32_t capacity) {
@@ -148,11 +163,12 @@ SortPlan make_sort_plan(uint32_t num_tiles);
 cudaError_t launch_preprocess(const FrameUniforms* d_frame, uint32_t n, const float4* pos,
                               const float4* scale, const float4* rot, const float4* color,
                               const float* sh_rest, uint32_t sh_degree,
-                              gs3d_projected_splat* out, uint32_t* counts, uint32_t* err,
-                              cudaStream_t s);
-cudaError_t launch_scan(const uint32_t* counts, uint32_t* offsets, uint32_t n,
-                        unsigned long long* status, uint32_t* tile_counter, uint32_t epoch,
-                        uint32_t* total_out, uint32_t* err, cudaStream_t s);
+                              gs3d_projected_splat* out, uint32_t* counts, uint32_t* depth_keys,
+                              uint32_t* depth_ids, uint32_t* err, cudaStream_t s);
+// Exclusive scan of counts[gather[i]] (counts[i] when gather is null).
+cudaError_t launch_scan(const uint32_t* counts, const uint32_t* gather, uint32_t* offsets,
+                        uint32_t n, unsigned long long* status, uint32_t* tile_counter,
+                        uint32_t epoch, uint32_t* total_out, uint32_t* err, cudaStream_t s);
 size_t scan_status_words(uint32_t n);
 cudaError_t launch_emit(const FrameUniforms* d_frame, uint32_t n,
                         const gs3d_projected_splat* proj, const uint32_t* offsets,
@@ -162,6 +178,24 @@ cudaError_t launch_sort(const SortPlan& plan, const uint32_t* ref_counter, uint3
                         uint2* keys_a, uint32_t* vals_a, uint2* keys_b, uint32_t* vals_b,
                         uint32_t* status, Ctrl* ctrl, int sm_count, cudaStream_t s);
 size_t sort_status_words(uint32_t capacity, int passes);
+// Tile-id passes of the fused rebin: histograms already in g_hist[p][256].
+cudaError_t launch_sort_tile_passes(const SortPlan& plan, const uint32_t* ref_counter,
+                                    uint32_t capacity, uint2* keys_a, uint32_t* vals_a,
+                                    uint2* keys_b, uint32_t* vals_b, uint32_t* status,
+                                    uint32_t* g_hist, uint32_t* part_counters, uint32_t* err,
+                                    int sm_count, cudaStream_t s);
+// Four 8-bit passes over 32-bit per-splat depth keys (count read on device).
+cudaError_t launch_sort_depth_keys(const uint32_t* count, uint32_t capacity, uint32_t* keys_a,
+                                   uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b,
+                                   uint32_t* status, uint32_t* g_hist, uint32_t* part_counters,
+                                   uint32_t* err, int sm_count, cudaStream_t s);
+// Emit in depth-sorted splat order + histograms of the tile-id digit places.
+cudaError_t launch_emit_sorted(const FrameUniforms* d_frame, uint32_t n,
+                               const gs3d_projected_splat* proj, const uint32_t* sorted_ids,
+                               const uint32_t* sorted_offsets, const uint32_t* ref_counter,
+                               uint32_t capacity, uint2* keys, uint32_t* values,
+                               const SortPlan& tile_plan, uint32_t* g_hist, uint32_t* err,
+                               cudaStream_t s);
 cudaError_t launch_identify(const uint2* keys, const uint32_t* ref_counter, uint32_t capacity,
                             uint32_t num_tiles, uint32_t* tile_offsets, uint32_t* err,
                             int sm_count, cudaStream_t s);

@@ -78,7 +78,8 @@ __global__ void __launch_bounds__(kThreads)
                       const float4* __restrict__ positions, const float4* __restrict__ scales,
                       const float4* __restrict__ rotations, const float4* __restrict__ colors,
                       const float* __restrict__ sh_rest, gs3d_projected_splat* __restrict__ out,
-                      uint32_t* __restrict__ counts, uint32_t* __restrict__ err) {
+                      uint32_t* __restrict__ counts, uint32_t* __restrict__ depth_keys,
+                      uint32_t* __restrict__ depth_ids, uint32_t* __restrict__ err) {
   constexpr int K = (DEG + 1) * (DEG + 1) - 1;
   constexpr int KC = 3 * K;  // floats of SH rest per splat
   extern __shared__ __align__(16) float s_sh[];
@@ -256,6 +257,10 @@ __global__ void __launch_bounds__(kThreads)
     o[2] = r2;
     reinterpret_cast<uint4*>(o)[3] = r3;
     counts[i] = count;
+    if (depth_keys != nullptr) {  // per-splat depth sort keys of the fused rebin
+      depth_keys[i] = valid ? __float_as_uint(-r0.z) : 0xffffffffu;
+      depth_ids[i] = i;
+    }
   }
 }
 
@@ -264,8 +269,8 @@ __global__ void __launch_bounds__(kThreads)
 cudaError_t launch_preprocess(const FrameUniforms* d_frame, uint32_t n, const float4* pos,
                               const float4* scale, const float4* rot, const float4* color,
                               const float* sh_rest, uint32_t sh_degree,
-                              gs3d_projected_splat* out, uint32_t* counts, uint32_t* err,
-                              cudaStream_t s) {
+                              gs3d_projected_splat* out, uint32_t* counts, uint32_t* depth_keys,
+                              uint32_t* depth_ids, uint32_t* err, cudaStream_t s) {
   const uint32_t blocks = (n + kThreads - 1) / kThreads;
   if (blocks == 0) return cudaSuccess;
   if (sh_rest == nullptr) sh_degree = 0;
@@ -274,20 +279,20 @@ cudaError_t launch_preprocess(const FrameUniforms* d_frame, uint32_t n, const fl
   switch (sh_degree) {
     case 0:
       preprocess_kernel<0><<<blocks, kThreads, 0, s>>>(d_frame, n, pos, scale, rot, color, nullptr,
-                                                       out, counts, err);
+                                                       out, counts, depth_keys, depth_ids, err);
       break;
     case 1:
       preprocess_kernel<1><<<blocks, kThreads, smem, s>>>(d_frame, n, pos, scale, rot, color,
-                                                          sh_rest, out, counts, err);
+                                                          sh_rest, out, counts, depth_keys, depth_ids, err);
       break;
     case 2:
       preprocess_kernel<2><<<blocks, kThreads, smem, s>>>(d_frame, n, pos, scale, rot, color,
-                                                          sh_rest, out, counts, err);
+                                                          sh_rest, out, counts, depth_keys, depth_ids, err);
       break;
     default: {
       // 45 floats x 256 splats = 46,080 B: inside the 48 KB default window.
       preprocess_kernel<3><<<blocks, kThreads, smem, s>>>(d_frame, n, pos, scale, rot, color,
-                                                          sh_rest, out, counts, err);
+                                                          sh_rest, out, counts, depth_keys, depth_ids, err);
       break;
     }
   }

@@ -35,7 +35,8 @@ __device__ __forceinline__ uint32_t warp_inclusive(uint32_t x, int lane) {
 }
 
 __global__ void __launch_bounds__(kThreads)
-    scan_kernel(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint32_t n,
+    scan_kernel(const uint32_t* __restrict__ in, const uint32_t* __restrict__ gather,
+                uint32_t* __restrict__ out, uint32_t n,
                 unsigned long long* __restrict__ status, uint32_t* __restrict__ ticket,
                 uint32_t epoch, uint32_t* __restrict__ total_out, uint32_t* __restrict__ err) {
   __shared__ uint32_t s_tile, s_prefix;
@@ -49,7 +50,10 @@ __global__ void __launch_bounds__(kThreads)
   const size_t base = (size_t)tile * kTile + (size_t)threadIdx.x * kItems;
 
   uint32_t v[kItems];
-  if (base + kItems <= n) {
+  if (gather != nullptr) {  // counts read through a permutation (fused rebin)
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) v[k] = (base + k < n) ? __ldg(in + __ldg(gather + base + k)) : 0u;
+  } else if (base + kItems <= n) {
     const uint4 a = __ldg(reinterpret_cast<const uint4*>(in + base));
     const uint4 b = __ldg(reinterpret_cast<const uint4*>(in + base) + 1);
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
@@ -156,15 +160,15 @@ __global__ void scan_empty_kernel(uint32_t* out, uint32_t* total_out) {
 
 size_t scan_status_words(uint32_t n) { return (n + kTile - 1) / kTile + 1; }
 
-cudaError_t launch_scan(const uint32_t* counts, uint32_t* offsets, uint32_t n,
-                        unsigned long long* status, uint32_t* tile_counter, uint32_t epoch,
-                        uint32_t* total_out, uint32_t* err, cudaStream_t s) {
+cudaError_t launch_scan(const uint32_t* counts, const uint32_t* gather, uint32_t* offsets,
+                        uint32_t n, unsigned long long* status, uint32_t* tile_counter,
+                        uint32_t epoch, uint32_t* total_out, uint32_t* err, cudaStream_t s) {
   if (n == 0) {
     scan_empty_kernel<<<1, 1, 0, s>>>(offsets, total_out);
     return cudaGetLastError();
   }
   const uint32_t tiles = (n + kTile - 1) / kTile;
-  scan_kernel<<<tiles, kThreads, 0, s>>>(counts, offsets, n, status, tile_counter, epoch,
+  scan_kernel<<<tiles, kThreads, 0, s>>>(counts, gather, offsets, n, status, tile_counter, epoch,
                                          total_out, err);
   return cudaGetLastError();
 }

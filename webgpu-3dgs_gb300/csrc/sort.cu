@@ -21,9 +21,14 @@
 // 8.  Passes alternate A->B->A; with an odd pass count the sorted result ends
 // in the B buffers and the host swaps the buffer names.
 //
+// The same pass kernel, instantiated for 32-bit keys, sorts the per-splat
+// depth keys of the fused rebin (rebin.cu).
+//
 // The order produced is identical to the reference's: lexicographic
 // (tile id, depth bits, emit position), since every pass is a stable
 // counting sort on one digit.
+#include <algorithm>
+
 #include "gs3d_internal.cuh"
 
 namespace gs3d {
@@ -35,16 +40,28 @@ constexpr int kItems = 16;
 constexpr uint32_t kPart = kThreads * kItems;  // 4096 keys per partition
 constexpr uint32_t kFlagAgg = 1u, kFlagInc = 2u;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
-constexpr size_t kPassSmem = (size_t)kPart * (sizeof(uint2) + sizeof(uint32_t)) +
-                             (size_t)kWarps * kRadixBins * sizeof(uint32_t);
 
-struct PassDev {
-  int word[kMaxSortPasses];
-  int shift[kMaxSortPasses];
+template <typename K>
+struct KeyOps;
+template <>
+struct KeyOps<uint2> {  // [hi = tile id, lo = depth bits]
+  static __device__ __forceinline__ uint2 sentinel() { return make_uint2(0xffffffffu, 0xffffffffu); }
+  static __device__ __forceinline__ uint32_t digit(uint2 k, int word, int shift) {
+    return ((word ? k.y : k.x) >> shift) & 0xffu;
+  }
+};
+template <>
+struct KeyOps<uint32_t> {
+  static __device__ __forceinline__ uint32_t sentinel() { return 0xffffffffu; }
+  static __device__ __forceinline__ uint32_t digit(uint32_t k, int, int shift) {
+    return (k >> shift) & 0xffu;
+  }
 };
 
-__device__ __forceinline__ uint32_t digit_of(uint2 k, int word, int shift) {
-  return ((word ? k.y : k.x) >> shift) & 0xffu;
+template <typename K>
+constexpr size_t pass_smem() {
+  return (size_t)kPart * (sizeof(K) + sizeof(uint32_t)) +
+         (size_t)kWarps * kRadixBins * sizeof(uint32_t);
 }
 
 __device__ __forceinline__ uint32_t warp_inclusive(uint32_t x, int lane) {
@@ -84,14 +101,19 @@ __device__ __forceinline__ uint32_t match_digit8(uint32_t d) {
   return peers;
 }
 
+struct PassDev {
+  int word[kMaxSortPasses];
+  int shift[kMaxSortPasses];
+};
+
 // Histogram of every sorted digit place + clear of the look-back status.
+template <typename K, int P>
 __global__ void __launch_bounds__(kThreads)
-    sort_histogram_kernel(const uint2* __restrict__ keys, const uint32_t* __restrict__ ref_counter,
-                          uint32_t capacity, int passes, PassDev pd, uint32_t* __restrict__ g_hist,
+    sort_histogram_kernel(const K* __restrict__ keys, const uint32_t* __restrict__ ref_counter,
+                          uint32_t capacity, PassDev pd, uint32_t* __restrict__ g_hist,
                           uint32_t* __restrict__ status, size_t status_stride) {
-  __shared__ uint32_t s_hist[kMaxSortPasses][kRadixBins];
-  for (int k = threadIdx.x; k < kMaxSortPasses * kRadixBins; k += kThreads)
-    (&s_hist[0][0])[k] = 0u;
+  __shared__ uint32_t s_hist[P][kRadixBins];
+  for (int k = threadIdx.x; k < P * kRadixBins; k += kThreads) (&s_hist[0][0])[k] = 0u;
   __syncthreads();
 
   const uint32_t R = live_refs(ref_counter, capacity);
@@ -99,42 +121,42 @@ __global__ void __launch_bounds__(kThreads)
   const size_t gtid = (size_t)blockIdx.x * kThreads + threadIdx.x;
   const size_t gstride = (size_t)gridDim.x * kThreads;
 
-  // clear status words of the partitions this sort will use
+  // clear the status words of the partitions this sort will use
   const size_t words = parts * kRadixBins;
-  for (size_t k = gtid; k < words * passes; k += gstride) {
+  for (size_t k = gtid; k < words * P; k += gstride) {
     const size_t p = k / words, o = k - p * words;
     status[p * status_stride + o] = 0u;
   }
 
-  const int lane = threadIdx.x & 31;
+  int word[P], shift[P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    word[p] = pd.word[p];
+    shift[p] = pd.shift[p];
+  }
   for (size_t base = (size_t)blockIdx.x * kThreads; base < R; base += gstride) {
     const size_t idx = base + threadIdx.x;
     const bool in = idx < R;
-    const uint2 k = in ? __ldg(keys + idx) : make_uint2(0u, 0u);
-    for (int p = 0; p < passes; ++p) {
-      const uint32_t d = digit_of(k, pd.word[p], pd.shift[p]);
-      const uint32_t act = __ballot_sync(0xffffffffu, in);
-      if (in) {
-        const uint32_t peers = __match_any_sync(act, d);
-        if ((__ffs(peers) - 1) == lane) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
-      }
-    }
+    const K k = in ? keys[idx] : KeyOps<K>::sentinel();
+#pragma unroll
+    for (int p = 0; p < P; ++p) hist_add_256(s_hist[p], KeyOps<K>::digit(k, word[p], shift[p]), in);
   }
   __syncthreads();
-  for (int k = threadIdx.x; k < passes * kRadixBins; k += kThreads) {
+  for (int k = threadIdx.x; k < P * kRadixBins; k += kThreads) {
     const uint32_t v = (&s_hist[0][0])[k];
     if (v) atomicAdd(g_hist + k, v);
   }
 }
 
+template <typename K>
 __global__ void __launch_bounds__(kThreads, 2)
-    onesweep_kernel(const uint2* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-                    uint2* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+    onesweep_kernel(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                    K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                     const uint32_t* __restrict__ ref_counter, uint32_t capacity, int word,
                     int shift, const uint32_t* __restrict__ hist, uint32_t* __restrict__ status,
                     uint32_t* __restrict__ part_counter, uint32_t* __restrict__ err) {
   extern __shared__ __align__(16) unsigned char smem[];
-  uint2* s_keys = reinterpret_cast<uint2*>(smem);
+  K* s_keys = reinterpret_cast<K*>(smem);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + kPart);
   uint32_t* s_whist = s_vals + kPart;  // [kWarps][256]
   __shared__ uint32_t s_bucket[kRadixBins], s_dstart[kRadixBins], s_dest[kRadixBins];
@@ -159,7 +181,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     const uint32_t count = min(kPart, R - base);
 
     // ---- load (warp-striped: lane-contiguous, coalesced) ----
-    uint2 key[kItems];
+    K key[kItems];
     uint32_t val[kItems];
     uint32_t dr[kItems];  // digit | rank-in-warp << 8
     const uint32_t wbase = base + warp * (32u * kItems);
@@ -167,10 +189,10 @@ __global__ void __launch_bounds__(kThreads, 2)
     for (int i = 0; i < kItems; ++i) {
       const uint32_t idx = wbase + i * 32u + lane;
       if (idx < R) {
-        key[i] = __ldg(keys_in + idx);
+        key[i] = keys_in[idx];
         val[i] = __ldg(vals_in + idx);
       } else {
-        key[i] = make_uint2(0xffffffffu, 0xffffffffu);  // digit 255, ranked last
+        key[i] = KeyOps<K>::sentinel();  // digit 255, ranked last
         val[i] = 0u;
       }
     }
@@ -179,7 +201,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     const uint32_t lt = lanemask_lt();
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
-      const uint32_t d = digit_of(key[i], word, shift);
+      const uint32_t d = KeyOps<K>::digit(key[i], word, shift);
       const uint32_t peers = match_digit8(d);
       const uint32_t prior = wh[d];
       __syncwarp();
@@ -244,8 +266,8 @@ __global__ void __launch_bounds__(kThreads, 2)
 
     // ---- write each digit run contiguously ----
     for (uint32_t j = tid; j < count; j += kThreads) {
-      const uint2 k = s_keys[j];
-      const uint32_t dst = s_dest[digit_of(k, word, shift)] + j;
+      const K k = s_keys[j];
+      const uint32_t dst = s_dest[KeyOps<K>::digit(k, word, shift)] + j;
       if (dst < R) {
         keys_out[dst] = k;
         vals_out[dst] = s_vals[j];
@@ -256,7 +278,92 @@ __global__ void __launch_bounds__(kThreads, 2)
   }
 }
 
-int g_onesweep_blocks_per_sm = 0;
+template <typename K>
+int& blocks_per_sm() {
+  static int v = 0;
+  return v;
+}
+
+template <typename K>
+cudaError_t onesweep_setup(int* per_sm) {
+  int& v = blocks_per_sm<K>();
+  if (v == 0) {
+    cudaError_t e = cudaFuncSetAttribute(onesweep_kernel<K>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)pass_smem<K>());
+    if (e != cudaSuccess) return e;
+    int n = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, onesweep_kernel<K>, kThreads,
+                                                      pass_smem<K>());
+    if (e != cudaSuccess) return e;
+    v = n > 0 ? n : 1;
+  }
+  *per_sm = v;
+  return cudaSuccess;
+}
+
+template <typename K>
+cudaError_t launch_histogram(int passes, const PassDev& pd, const K* keys,
+                             const uint32_t* ref_counter, uint32_t capacity, uint32_t* g_hist,
+                             uint32_t* status, size_t stride, int grid, cudaStream_t s) {
+#define GS3D_HIST_CASE(P)                                                                    \
+  case P:                                                                                    \
+    sort_histogram_kernel<K, P><<<grid, kThreads, 0, s>>>(keys, ref_counter, capacity, pd,   \
+                                                          g_hist, status, stride);           \
+    break;
+  switch (passes) {
+    GS3D_HIST_CASE(1)
+    GS3D_HIST_CASE(2)
+    GS3D_HIST_CASE(3)
+    GS3D_HIST_CASE(4)
+    GS3D_HIST_CASE(5)
+    GS3D_HIST_CASE(6)
+    GS3D_HIST_CASE(7)
+    GS3D_HIST_CASE(8)
+    default:
+      return cudaErrorInvalidValue;
+  }
+#undef GS3D_HIST_CASE
+  return cudaGetLastError();
+}
+
+// Runs `plan` over keys/vals A<->B; the histogram of every pass must be in
+// g_hist[p][256] (computed here unless hist_ready) and status must hold
+// sort_status_words(capacity, passes) words.
+template <typename K>
+cudaError_t run_passes(const SortPlan& plan, const uint32_t* ref_counter, uint32_t capacity,
+                       K* keys_a, uint32_t* vals_a, K* keys_b, uint32_t* vals_b,
+                       uint32_t* status, uint32_t* g_hist, uint32_t* part_counters,
+                       uint32_t* err, bool hist_ready, int sm_count, cudaStream_t s) {
+  int per_sm = 0;
+  cudaError_t e = onesweep_setup<K>(&per_sm);
+  if (e != cudaSuccess) return e;
+  const size_t parts_cap = ((size_t)capacity + kPart - 1) / kPart + 1;
+  const size_t stride = parts_cap * kRadixBins;
+  PassDev pd{};
+  for (int p = 0; p < plan.passes; ++p) {
+    pd.word[p] = plan.word[p];
+    pd.shift[p] = plan.shift[p];
+  }
+  if (!hist_ready) {
+    e = launch_histogram<K>(plan.passes, pd, keys_a, ref_counter, capacity, g_hist, status,
+                            stride, sm_count * 4, s);
+  } else {
+    e = cudaMemsetAsync(status, 0, stride * plan.passes * sizeof(uint32_t), s);
+  }
+  if (e != cudaSuccess) return e;
+  const int grid = (int)std::min<size_t>((size_t)sm_count * per_sm, parts_cap);
+  for (int p = 0; p < plan.passes; ++p) {
+    const bool even = (p % 2) == 0;
+    onesweep_kernel<K><<<grid, kThreads, pass_smem<K>(), s>>>(
+        even ? keys_a : keys_b, even ? vals_a : vals_b, even ? keys_b : keys_a,
+        even ? vals_b : vals_a, ref_counter, capacity, plan.word[p], plan.shift[p],
+        g_hist + (size_t)p * kRadixBins, status + (size_t)p * stride, part_counters + p, err);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
 
 }  // namespace
 
@@ -287,48 +394,37 @@ size_t sort_status_words(uint32_t capacity, int passes) {
 cudaError_t launch_sort(const SortPlan& plan, const uint32_t* ref_counter, uint32_t capacity,
                         uint2* keys_a, uint32_t* vals_a, uint2* keys_b, uint32_t* vals_b,
                         uint32_t* status, Ctrl* ctrl, int sm_count, cudaStream_t s) {
-  if (g_onesweep_blocks_per_sm == 0) {
-    cudaError_t e = cudaFuncSetAttribute(onesweep_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kPassSmem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, onesweep_kernel, kThreads,
-                                                      kPassSmem);
-    if (e != cudaSuccess) return e;
-    g_onesweep_blocks_per_sm = per_sm > 0 ? per_sm : 1;
-  }
-  // counters and histograms for this sort
   cudaError_t e = cudaMemsetAsync(ctrl->sort_part_counter, 0,
                                   sizeof(ctrl->sort_part_counter) + sizeof(ctrl->pad) +
                                       sizeof(ctrl->sort_hist),
                                   s);
   if (e != cudaSuccess) return e;
-  const size_t parts_cap = ((size_t)capacity + kPart - 1) / kPart + 1;
-  const size_t stride = parts_cap * kRadixBins;
-  PassDev pd{};
-  for (int p = 0; p < plan.passes; ++p) {
-    pd.word[p] = plan.word[p];
-    pd.shift[p] = plan.shift[p];
+  return run_passes<uint2>(plan, ref_counter, capacity, keys_a, vals_a, keys_b, vals_b, status,
+                           &ctrl->sort_hist[0][0], ctrl->sort_part_counter, &ctrl->error,
+                           false, sm_count, s);
+}
+
+cudaError_t launch_sort_tile_passes(const SortPlan& plan, const uint32_t* ref_counter,
+                                    uint32_t capacity, uint2* keys_a, uint32_t* vals_a,
+                                    uint2* keys_b, uint32_t* vals_b, uint32_t* status,
+                                    uint32_t* g_hist, uint32_t* part_counters, uint32_t* err,
+                                    int sm_count, cudaStream_t s) {
+  return run_passes<uint2>(plan, ref_counter, capacity, keys_a, vals_a, keys_b, vals_b, status,
+                           g_hist, part_counters, err, true, sm_count, s);
+}
+
+cudaError_t launch_sort_depth_keys(const uint32_t* count, uint32_t capacity, uint32_t* keys_a,
+                                   uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b,
+                                   uint32_t* status, uint32_t* g_hist, uint32_t* part_counters,
+                                   uint32_t* err, int sm_count, cudaStream_t s) {
+  SortPlan plan{};
+  plan.passes = 4;
+  for (int p = 0; p < 4; ++p) {
+    plan.word[p] = 1;
+    plan.shift[p] = 8 * p;
   }
-  sort_histogram_kernel<<<sm_count * 4, kThreads, 0, s>>>(keys_a, ref_counter, capacity,
-                                                          plan.passes, pd, &ctrl->sort_hist[0][0],
-                                                          status, stride);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  const size_t max_grid = (size_t)sm_count * g_onesweep_blocks_per_sm;
-  const int grid = (int)std::min(max_grid, parts_cap);
-  for (int p = 0; p < plan.passes; ++p) {
-    const bool even = (p % 2) == 0;
-    onesweep_kernel<<<grid, kThreads, kPassSmem, s>>>(
-        even ? keys_a : keys_b, even ? vals_a : vals_b, even ? keys_b : keys_a,
-        even ? vals_b : vals_a, ref_counter, capacity, plan.word[p], plan.shift[p],
-        ctrl->sort_hist[p], status + (size_t)p * stride, &ctrl->sort_part_counter[p],
-        &ctrl->error);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  return run_passes<uint32_t>(plan, count, capacity, keys_a, vals_a, keys_b, vals_b, status,
+                              g_hist, part_counters, err, false, sm_count, s);
 }
 
 }  // namespace gs3d

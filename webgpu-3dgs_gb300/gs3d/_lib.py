@@ -26,6 +26,11 @@ STATUS_NAMES = {
     ERR_NO_DEVICE: "GS3D_ERR_NO_DEVICE",
 }
 
+FLAG_STAGEWISE_REBIN = 1
+FLAG_STAGE_TIMING = 2
+STAGE_NAMES = ["preprocess-splats", "depth-sort", "prefix-scan", "emit-tile-refs", "radix-sort",
+               "identify-tile-ranges", "rasterize-tiles"]
+
 # named buffers (gs3d.h, gs3d_buffer)
 BUFFERS = {
     "splat_positions": 0, "splat_scales": 1, "splat_rotations": 2, "splat_colors": 3,
@@ -74,6 +79,8 @@ SIGNATURES = {
     "gs3d_identify_tile_ranges": ([_P], _I),
     "gs3d_rasterize_tiles": ([_P], _I),
     "gs3d_rebin": ([_P, C.POINTER(Camera_t), _U32, _U32], _I),
+    "gs3d_set_flags": ([_P, _U32], _I),
+    "gs3d_read_stage_times": ([_P, C.POINTER(C.c_double), C.POINTER(_U32)], _I),
     "gs3d_synchronize": ([_P], _I),
     "gs3d_buffer_info": ([_P, _I, C.POINTER(C.c_void_p), C.POINTER(_SZ)], _I),
     "gs3d_read_buffer": ([_P, _I, _P, _SZ], _I),

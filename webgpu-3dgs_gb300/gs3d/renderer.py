@@ -132,6 +132,12 @@ class GaussianSplatRenderer:
         self.scene.tiles = [ox.value, oy.value]
         return ox.value, oy.value
 
+    def setStagewise(self, on: bool) -> None:
+        """Selects the stage-wise rebin (the six reference stages in order)
+        instead of the fused default; both give identical sorted keys,
+        values, tile ranges and images."""
+        self._call("gs3d_set_flags", _lib.FLAG_STAGEWISE_REBIN if on else 0)
+
     def setAlwaysRebin(self, on: bool) -> None:
         self.alwaysRebin = bool(on)
 
