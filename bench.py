@@ -171,12 +171,37 @@ def run_ours(args, rank, world):
         check(lib.gs3d_ref_count(ctx, C.byref(r)))
         refs.append(r.value)
 
-    def timed(stagewise: bool):
-        flags = _lib.FLAG_STAGE_TIMING | (_lib.FLAG_STAGEWISE_REBIN if stagewise else 0)
-        check(lib.gs3d_set_flags(ctx, flags))
-        for _ in range(args.warmup):
+    B = args.batch
+    batches = []
+    for b0 in range(0, len(cams), B):
+        arr = (_lib.View_t * min(B, len(cams) - b0))()
+        for i in range(len(arr)):
+            arr[i].camera = cam_structs[b0 + i]
+            arr[i].scene = 0
+            arr[i].width, arr[i].height = WIDTH, HEIGHT
+        batches.append(arr)
+
+    def run_step(path):
+        if path == "batched":
+            for arr in batches:
+                check(lib.gs3d_rebin_batch(ctx, C.cast(arr, C.c_void_p), len(arr)))
+        else:
             for cs in cam_structs:
                 check(lib.gs3d_rebin(ctx, C.byref(cs), WIDTH, HEIGHT))
+
+    def timed(path: str):
+        flags = _lib.FLAG_STAGE_TIMING | (_lib.FLAG_STAGEWISE_REBIN if path == "stagewise" else 0)
+        check(lib.gs3d_set_flags(ctx, flags))
+        check(lib.gs3d_set_schedule(ctx, _lib.SCHEDULE_KEY_COUNT if path == "batched"
+                                    else _lib.SCHEDULE_ROW_MAJOR))
+        for _ in range(3):  # size the key buffers for this path's batch
+            run_step(path)
+            rc = lib.gs3d_synchronize(ctx)
+            if rc != _lib.ERR_CAPACITY:
+                check(rc)
+                break
+        for _ in range(args.warmup):
+            run_step(path)
         check(lib.gs3d_synchronize(ctx))
         check(lib.gs3d_read_stage_times(ctx, None, None))  # reset
         start, stop = (torch.cuda.Event(enable_timing=True) for _ in range(2))
@@ -186,8 +211,7 @@ def run_ours(args, rank, world):
         with ClockSampler(dev) as clocks:
             start.record(stream)
             for _ in range(args.steps):
-                for cs in cam_structs:
-                    check(lib.gs3d_rebin(ctx, C.byref(cs), WIDTH, HEIGHT))
+                run_step(path)
             stop.record(stream)
             torch.cuda.synchronize()
         check(lib.gs3d_synchronize(ctx))
@@ -195,6 +219,7 @@ def run_ours(args, rank, world):
         cnt = (C.c_uint32 * 7)()
         check(lib.gs3d_read_stage_times(ctx, ms, cnt))
         check(lib.gs3d_set_flags(ctx, 0))
+        check(lib.gs3d_set_schedule(ctx, _lib.SCHEDULE_ROW_MAJOR))
         total = start.elapsed_time(stop)
         if world > 1:
             t = torch.tensor([total], device="cuda")
@@ -202,11 +227,12 @@ def run_ours(args, rank, world):
             total = float(t.item())
         views = args.steps * len(cam_structs)
         per_stage = {name: (ms[i] / views, cnt[i] / views) for i, name in
-                     enumerate(_lib.STAGE_NAMES) if cnt[i]}
+                     enumerate(_lib.STAGE_NAMES) if cnt[i]}  # per view
         return total, per_stage, clocks.summary()
 
-    fused_ms, fused_stages, clocks = timed(False)
-    stagewise_ms, stagewise_stages, _ = timed(True)
+    batched_ms, batched_stages, clocks = timed("batched")
+    fused_ms, fused_stages, _ = timed("fused")
+    stagewise_ms, stagewise_stages, _ = timed("stagewise")
     views = args.steps * len(cam_structs)
 
     # ---- e2e: public entry point, host camera in, pinned host image out ----
@@ -231,12 +257,13 @@ def run_ours(args, rank, world):
     lib.gs3d_destroy(ctx)
 
     tiles = (WIDTH // TILE) * -(-HEIGHT // TILE)
-    tile_passes = ((tiles - 1).bit_length() + 7) // 8
+    tile_passes = ((tiles - 1).bit_length() + 7) // 8          # one view
+    batch_tile_passes = ((tiles * B - 1).bit_length() + 7) // 8  # B views: global tile ids
     mean_R = float(np.mean(refs))
     peak, peak_kind = peaks()
 
-    def roof(stages, fused):
-        algo = algorithmic_bytes(N_SPLATS, mean_R, tiles, tile_passes, 45, fused)
+    def roof(stages, fused, passes=tile_passes):
+        algo = algorithmic_bytes(N_SPLATS, mean_R, tiles, passes, 45, fused)
         out = {}
         for name, (ms, n) in stages.items():
             gbs = algo[name] / (ms * 1e-3) / 1e9
@@ -244,20 +271,24 @@ def run_ours(args, rank, world):
                          "frac_hbm": round(gbs / peak, 3)}
         return out
 
-    fused_roof = roof(fused_stages, True)
-    hbm = [s for s in fused_roof if s != "rasterize-tiles"]
-    dom = max(hbm, key=lambda s: fused_roof[s]["ms"])
-    launches = 1 + 5 + 1 + 1 + tile_passes + 1 + 1  # preprocess, depth sort, scan, emit, ...
+    batched_roof = roof(batched_stages, True, batch_tile_passes)
+    hbm = [s for s in batched_roof if s != "rasterize-tiles"]
+    dom = max(hbm, key=lambda s: batched_roof[s]["ms"])
+    # kernels of one batched rebin: preprocess, depth sort (histogram + 4 passes), scan, emit,
+    # tile-digit passes, identify, schedule (keys + histogram + 2 passes), raster
+    launches_per_batch = 1 + 5 + 1 + 1 + batch_tile_passes + 1 + 4 + 1
     return {
-        "value": views * world / (fused_ms * 1e-3), "ms_per_step": fused_ms / args.steps,
-        "views": views, "per_stage": fused_roof, "dominant": dom, "peak": peak,
+        "value": views * world / (batched_ms * 1e-3), "ms_per_step": batched_ms / args.steps,
+        "views": views, "per_stage": batched_roof, "dominant": dom, "peak": peak,
+        "fused_value": views * world / (fused_ms * 1e-3), "fused_stages": roof(fused_stages, True),
         "peak_kind": peak_kind, "mean_refs": mean_R, "tile_passes": tile_passes,
         "clocks": clocks,
         "stagewise_value": views * world / (stagewise_ms * 1e-3),
         "stagewise_stages": roof(stagewise_stages, False),
         "e2e_value": views * world / (e2e_ms * 1e-3), "e2e_wall_value": views / e2e_wall,
         "h2d": 288 * len(cam_structs), "d2h": img_bytes * len(cam_structs),
-        "launches_per_view": launches,
+        "launches_per_step": launches_per_batch * len(batches),
+        "tile_passes_batched": batch_tile_passes,
     }
 
 
@@ -283,6 +314,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--views", type=int, default=64)
+    ap.add_argument("--batch", type=int, default=16, help="views per batched rebin")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -325,21 +357,25 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "path": "single-view fused rebin",
+            "config": {"workload": WORKLOAD,
+                       "path": f"batched fused rebin, {args.batch} views per launch sequence, "
+                               "key-count raster schedule",
                        "views_per_step": args.views, "l2": "inputs larger than L2 (no flush)",
                        "mean_refs_per_view": res["mean_refs"],
-                       "tile_digit_passes": res["tile_passes"],
-                       "stagewise_views_per_s": res["stagewise_value"]},
+                       "tile_digit_passes": res["tile_passes_batched"],
+                       "single_view_fused_views_per_s": res["fused_value"],
+                       "plain_stagewise_views_per_s": res["stagewise_value"]},
             "roofline": {"bound": "hbm", "kernel": res["dominant"], "achieved": dom["gbs"],
                          "peak": res["peak"], "unit": "GB/s", "frac": dom["frac_hbm"],
                          "peak_kind": res["peak_kind"], "traffic": None},
             "stages": res["per_stage"],
-            "stages_stagewise": res["stagewise_stages"],
+            "stages_single_view_fused": res["fused_stages"],
+            "stages_plain_stagewise": res["stagewise_stages"],
             "cpu_baseline": cpu,
             "e2e": {"value": res["e2e_value"], "unit": "views/s",
                     "h2d_bytes_per_step": res["h2d"], "d2h_bytes_per_step": res["d2h"],
                     "wall_value": res["e2e_wall_value"]},
-            "gpu_launches": res["launches_per_view"] * res["views"],
+            "gpu_launches": res["launches_per_step"] * args.steps,
             "clocks": res["clocks"],
         }
         print(json.dumps(out))

@@ -103,6 +103,33 @@ typedef struct gs3d_config {
 #define GS3D_STAGE_RASTER     6  /* rasterize-tiles                           */
 #define GS3D_STAGE_COUNT      7
 
+/* One view of a batched rebin (extension: the reference renders one view per
+ * frame).  scene 0 is the gs3d_set_splats scene; others come from
+ * gs3d_add_scene. */
+typedef struct gs3d_view {
+    gs3d_camera camera;
+    uint32_t scene;
+    uint32_t width, height;
+    uint32_t reserved;
+} gs3d_view;
+
+/* Where a view of the last rebin lives in the batch-wide buffers: its image
+ * starts at pixel pixel_offset of the splat target, its tiles are global
+ * tiles [tile_base, tile_base + tiles_x*tiles_y) of tile_offsets, its
+ * splat-views are [splat_base, splat_base + splat_count) of projected_splats,
+ * and its sorted values hold splat_base + splat id. */
+typedef struct gs3d_view_info {
+    uint64_t pixel_offset;
+    uint32_t width, height;
+    uint32_t tiles_x, tiles_y, tile_base;
+    uint32_t splat_base, splat_count;
+    uint32_t scene;
+} gs3d_view_info;
+
+/* Raster work order (the persistent raster CTAs pull tiles from a queue). */
+#define GS3D_SCHEDULE_ROW_MAJOR 0u  /* the reference's dispatch order          */
+#define GS3D_SCHEDULE_KEY_COUNT 1u  /* decreasing key count (longest first)    */
+
 /* Named device buffers (BufferManager names, GaussianSplatRenderer.ts:338-465). */
 typedef enum gs3d_buffer {
     GS3D_BUF_SPLAT_POSITIONS   = 0,  /* vec4 f32 x N                               */
@@ -149,6 +176,15 @@ int gs3d_set_splats(struct gs3d_ctx* ctx, uint32_t n,
                     const float* rotations, const float* colors,
                     const float* sh_rest, uint32_t sh_degree, int memory);
 
+/* Adds another resident scene for batched rendering (extension; the
+ * reference holds one scene).  Arguments as gs3d_set_splats; the first scene
+ * added to an empty context becomes scene 0. */
+int gs3d_add_scene(struct gs3d_ctx* ctx, uint32_t n,
+                   const float* positions, const float* scales,
+                   const float* rotations, const float* colors,
+                   const float* sh_rest, uint32_t sh_degree, int memory,
+                   uint32_t* out_scene);
+
 /* setTileSize (GaussianSplatRenderer.ts:301-317): clamps to the device limit
  * (tile_w * tile_h <= 1024) and reports the size in use. */
 int gs3d_set_tile_size(struct gs3d_ctx* ctx, uint32_t tile_w, uint32_t tile_h,
@@ -180,6 +216,17 @@ int gs3d_set_flags(struct gs3d_ctx* ctx, uint32_t flags);
  * device milliseconds and stage executions accumulated since the last call
  * (GS3D_STAGE_COUNT entries each; either pointer may be NULL) and resets. */
 int gs3d_read_stage_times(struct gs3d_ctx* ctx, double* ms, uint32_t* executions);
+
+/* Batched rebin (extension): renders n_views views, of any resident scenes
+ * and sizes, in one launch sequence.  Per view the sorted keys (hi = the
+ * view's tile_base + local tile id), values (splat_base + splat id),
+ * tile_offsets and image equal a single-view rebin of that view. */
+int gs3d_rebin_batch(struct gs3d_ctx* ctx, const gs3d_view* views, uint32_t n_views);
+int gs3d_get_view_info(struct gs3d_ctx* ctx, uint32_t view, gs3d_view_info* out);
+
+/* Selects the raster work order (GS3D_SCHEDULE_*); the image is the same
+ * under every schedule. */
+int gs3d_set_schedule(struct gs3d_ctx* ctx, uint32_t schedule);
 
 /* Waits for the context's stream and reports latched device errors.  After
  * GS3D_ERR_CAPACITY the key buffers have already been grown to the observed

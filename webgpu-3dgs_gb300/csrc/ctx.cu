@@ -16,6 +16,10 @@
 // buffers start at N * max_tiles_per_splat entries like the reference but
 // overflow is detected on the device and reported, after which the buffers
 // are grown and the caller re-issues the rebin.
+//
+// Every rebin runs over a device-side view table (ViewDesc); a single-view
+// rebin is a batch of one, gs3d_rebin_batch renders many views, of several
+// scenes and uneven sizes, in one launch sequence.
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
@@ -32,11 +36,17 @@ namespace {
 
 // Look-back status words carry 30-bit values, which bounds the live count.
 constexpr uint32_t kMaxCapacity = (1u << 30) - 1u;
-constexpr int kFrameSlots = 8;
+constexpr int kUploadSlots = 8;
+constexpr uint32_t kPreBlock = 256;  // preprocess threads per block
 
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+};
+
+struct SceneBufs {
+  uint32_t n = 0, sh_degree = 0;
+  DevBuf pos, scale, rot, color, sh;
 };
 
 __global__ void probe_kernel(int* out) {
@@ -54,29 +64,32 @@ struct gs3d_ctx {
 
   uint32_t tile_w = 16, tile_h = 16, max_tiles_per_splat = 16;
   uint32_t flags = 0;
+  uint32_t schedule = GS3D_SCHEDULE_ROW_MAJOR;
 
-  // scene (SceneSyncer buffers)
+  std::vector<SceneBufs> scenes;  // scene 0 = the gs3d_set_splats scene
   bool have_scene = false;
-  uint32_t n = 0, sh_degree = 0;
-  DevBuf pos, scale, rot, color, sh;
 
-  // binning (GaussianSplatRenderer buffers)
+  // binning buffers, sized for the largest batch seen
   DevBuf proj, counts, offsets, ref_counter;
   DevBuf keys_a, vals_a, keys_b, vals_b;
   uint32_t capacity = 0;
   DevBuf scan_status, sort_status;
   uint32_t scan_epoch = 0;
-  // fused rebin: per-splat depth keys/ids (ping-pong), offsets in depth order
   DevBuf depth_keys_a, depth_ids_a, depth_keys_b, depth_ids_b, sorted_offsets, depth_status;
-
-  // frame
-  bool have_camera = false;
-  DevBuf frame;
-  FrameUniforms* h_frames = nullptr;  // pinned ring
-  cudaEvent_t frame_ev[kFrameSlots] = {};
-  int frame_slot = 0;
-  uint32_t W = 0, H = 0, tiles_x = 0, tiles_y = 0;
   DevBuf tile_offsets, image, tile_costs;
+  DevBuf sched_keys_a, sched_keys_b, sched_order_a, sched_order_b, sched_status;
+
+  // the current batch (a single-view frame is a batch of one)
+  bool have_camera = false;
+  std::vector<ViewDesc> views;       // host copy
+  std::vector<gs3d_view_info> info;  // per-view layout
+  uint32_t total_splats = 0, total_tiles = 0, total_blocks = 0, max_sh = 0;
+  uint64_t total_pixels = 0;
+  DevBuf d_views;
+  ViewDesc* h_upload = nullptr;  // pinned ring of view tables
+  size_t upload_cap = 0;         // views per slot
+  cudaEvent_t upload_ev[kUploadSlots] = {};
+  int upload_slot = 0;
 
   DevBuf ctrl;
   uint32_t* h_word = nullptr;  // pinned scratch for small reads
@@ -114,10 +127,16 @@ int cuda_fail(gs3d_ctx* c, cudaError_t e, const char* what) {
   return fail(c, code, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
 }
 
-#define CK(expr, what)                                   \
-  do {                                                   \
-    cudaError_t e_ = (expr);                             \
+#define CK(expr, what)                                    \
+  do {                                                    \
+    cudaError_t e_ = (expr);                              \
     if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+  } while (0)
+
+#define TRY(expr)                 \
+  do {                            \
+    const int r_ = (expr);        \
+    if (r_ != GS3D_OK) return r_; \
   } while (0)
 
 void release(DevBuf& b) {
@@ -146,11 +165,9 @@ int ensure(gs3d_ctx* c, DevBuf& b, size_t bytes, const char* name) {
   return GS3D_OK;
 }
 
-#define TRY(expr)                 \
-  do {                            \
-    const int r_ = (expr);        \
-    if (r_ != GS3D_OK) return r_; \
-  } while (0)
+uint32_t* u32(DevBuf& b) { return static_cast<uint32_t*>(b.p); }
+Ctrl* ctrl_of(gs3d_ctx* c) { return static_cast<Ctrl*>(c->ctrl.p); }
+ViewDesc* dviews(gs3d_ctx* c) { return static_cast<ViewDesc*>(c->d_views.p); }
 
 int ensure_key_capacity(gs3d_ctx* c, uint64_t want) {
   if (want > kMaxCapacity)
@@ -158,26 +175,35 @@ int ensure_key_capacity(gs3d_ctx* c, uint64_t want) {
                 (unsigned long long)want, kMaxCapacity);
   if (want <= c->capacity && c->keys_a.p) return GS3D_OK;
   const uint32_t cap = (uint32_t)std::max<uint64_t>(want, 1);
-  TRY(ensure(c, c->keys_a, (size_t)cap * sizeof(uint2), "sort_keys_a"));
-  TRY(ensure(c, c->keys_b, (size_t)cap * sizeof(uint2), "sort_keys_b"));
-  TRY(ensure(c, c->vals_a, (size_t)cap * sizeof(uint32_t), "sort_values_a"));
-  TRY(ensure(c, c->vals_b, (size_t)cap * sizeof(uint32_t), "sort_values_b"));
+  const size_t alloc = sort_capacity_round(cap);  // sort passes fetch whole partitions
+  TRY(ensure(c, c->keys_a, alloc * sizeof(uint2), "sort_keys_a"));
+  TRY(ensure(c, c->keys_b, alloc * sizeof(uint2), "sort_keys_b"));
+  TRY(ensure(c, c->vals_a, alloc * sizeof(uint32_t), "sort_values_a"));
+  TRY(ensure(c, c->vals_b, alloc * sizeof(uint32_t), "sort_values_b"));
   TRY(ensure(c, c->sort_status, sort_status_words(cap, kMaxSortPasses) * sizeof(uint32_t),
              "sort look-back status"));
   c->capacity = cap;
   return GS3D_OK;
 }
 
-int set_device(gs3d_ctx* c) {
-  CK(cudaSetDevice(c->device), "cudaSetDevice");
+// Per-splat-view buffers for a batch of `m` splat-views.
+int ensure_splat_buffers(gs3d_ctx* c, uint32_t m) {
+  TRY(ensure(c, c->proj, (size_t)m * sizeof(gs3d_projected_splat), "projected_splats"));
+  TRY(ensure(c, c->counts, (size_t)m * 4, "splat_ref_counts"));
+  TRY(ensure(c, c->offsets, ((size_t)m + 1) * 4, "splat_ref_offsets"));
+  TRY(ensure(c, c->scan_status, scan_status_words(m) * 8, "scan look-back status"));
+  const size_t md = sort_capacity_round(std::max<uint32_t>(m, 1));
+  TRY(ensure(c, c->depth_keys_a, md * 4, "depth keys"));
+  TRY(ensure(c, c->depth_keys_b, md * 4, "depth keys"));
+  TRY(ensure(c, c->depth_ids_a, md * 4, "depth ids"));
+  TRY(ensure(c, c->depth_ids_b, md * 4, "depth ids"));
+  TRY(ensure(c, c->sorted_offsets, ((size_t)m + 1) * 4, "depth-ordered offsets"));
+  TRY(ensure(c, c->depth_status, sort_status_words(m, 4) * 4, "depth sort status"));
   return GS3D_OK;
 }
 
-Ctrl* ctrl_of(gs3d_ctx* c) { return static_cast<Ctrl*>(c->ctrl.p); }
-
-int require_frame(gs3d_ctx* c, const char* stage) {
-  if (!c->have_scene) return fail(c, GS3D_ERR_STATE, "%s: no splats set", stage);
-  if (!c->have_camera) return fail(c, GS3D_ERR_STATE, "%s: no camera set", stage);
+int set_device(gs3d_ctx* c) {
+  CK(cudaSetDevice(c->device), "cudaSetDevice");
   return GS3D_OK;
 }
 
@@ -222,7 +248,7 @@ int drain_timing(gs3d_ctx* c) {
   return GS3D_OK;
 }
 
-// RAII pair of events around one stage when timing is on.
+// A pair of events around one stage when timing is on.
 struct StageScope {
   gs3d_ctx* c;
   int stage;
@@ -250,15 +276,271 @@ int sync_and_check(gs3d_ctx* c) {
   return check_device_errors(c);
 }
 
+int upload_scene(gs3d_ctx* c, SceneBufs& sc, uint32_t n, const float* positions,
+                 const float* scales, const float* rotations, const float* colors,
+                 const float* sh_rest, uint32_t sh_degree, int memory) {
+  if (memory != 0 && memory != 1) return fail(c, GS3D_ERR_INVALID_ARG, "memory must be 0 or 1");
+  if (sh_degree > 3) return fail(c, GS3D_ERR_INVALID_ARG, "sh_degree %u > 3", sh_degree);
+  if (n > 0 && (!positions || !scales || !rotations || !colors))
+    return fail(c, GS3D_ERR_INVALID_ARG, "null splat array");
+  if (n > 0 && sh_degree > 0 && !sh_rest)
+    return fail(c, GS3D_ERR_INVALID_ARG, "sh_degree %u needs sh_rest", sh_degree);
+  if (n > (1u << 30)) return fail(c, GS3D_ERR_INVALID_ARG, "too many splats (%u)", n);
+  TRY(set_device(c));
+  const size_t v4 = (size_t)n * 16;
+  const uint32_t kc = 3u * ((sh_degree + 1) * (sh_degree + 1) - 1);
+  TRY(ensure(c, sc.pos, v4, "splat_positions"));
+  TRY(ensure(c, sc.scale, v4, "splat_scales"));
+  TRY(ensure(c, sc.rot, v4, "splat_rotations"));
+  TRY(ensure(c, sc.color, v4, "splat_colors"));
+  if (kc) TRY(ensure(c, sc.sh, (size_t)n * kc * sizeof(float), "splat_sh_rest"));
+  const cudaMemcpyKind kind = memory ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (n) {
+    CK(cudaMemcpyAsync(sc.pos.p, positions, v4, kind, c->stream), "upload positions");
+    CK(cudaMemcpyAsync(sc.scale.p, scales, v4, kind, c->stream), "upload scales");
+    CK(cudaMemcpyAsync(sc.rot.p, rotations, v4, kind, c->stream), "upload rotations");
+    CK(cudaMemcpyAsync(sc.color.p, colors, v4, kind, c->stream), "upload colors");
+    if (kc)
+      CK(cudaMemcpyAsync(sc.sh.p, sh_rest, (size_t)n * kc * sizeof(float), kind, c->stream),
+         "upload sh_rest");
+  }
+  CK(cudaStreamSynchronize(c->stream), "splat upload");
+  sc.n = n;
+  sc.sh_degree = sh_degree;
+  return GS3D_OK;
+}
+
+// Builds the batch layout on the host, sizes every buffer for it and uploads
+// the view table through a pinned ring slot (stream ordered).
+int set_views(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views) {
+  if (n_views == 0 || !views) return fail(c, GS3D_ERR_INVALID_ARG, "empty view list");
+  std::vector<ViewDesc> vds(n_views, ViewDesc{});
+  std::vector<gs3d_view_info> infos(n_views, gs3d_view_info{});
+  uint64_t splats = 0, tiles = 0, pixels = 0, blocks = 0;
+  uint32_t max_sh = 0;
+  for (uint32_t v = 0; v < n_views; ++v) {
+    const gs3d_view& in = views[v];
+    if (in.scene >= c->scenes.size())
+      return fail(c, GS3D_ERR_INVALID_ARG, "view %u names unknown scene %u", v, in.scene);
+    const SceneBufs& sc = c->scenes[in.scene];
+    const uint32_t w = std::max<uint32_t>(1, in.width);   // GaussianSplatRenderer.ts:1040
+    const uint32_t h = std::max<uint32_t>(1, in.height);
+    const uint32_t tx = (w + c->tile_w - 1) / c->tile_w;  // :1042-1043
+    const uint32_t ty = (h + c->tile_h - 1) / c->tile_h;
+    ViewDesc& d = vds[v];
+    FrameUniforms& f = d.f;
+    f.cam = in.camera;
+    f.tile_count[0] = tx;
+    f.tile_count[1] = ty;
+    f.splat_count = sc.n;
+    f.num_tiles = tx * ty;
+    f.inv_tile[0] = (float)(1.0 / c->tile_w);  // :1127-1128, f64 division stored as f32
+    f.inv_tile[1] = (float)(1.0 / c->tile_h);
+    f.viewport[0] = w;
+    f.viewport[1] = h;
+    f.tile_size[0] = c->tile_w;
+    f.tile_size[1] = c->tile_h;
+    f.tile_base = (uint32_t)tiles;
+    d.pos = static_cast<const float4*>(sc.pos.p);
+    d.scale = static_cast<const float4*>(sc.scale.p);
+    d.rot = static_cast<const float4*>(sc.rot.p);
+    d.color = static_cast<const float4*>(sc.color.p);
+    d.sh = sc.sh_degree ? static_cast<const float*>(sc.sh.p) : nullptr;
+    d.sh_degree = sc.sh_degree;
+    d.splat_base = (uint32_t)splats;
+    d.block_base = (uint32_t)blocks;
+    d.pixel_base = pixels;
+    gs3d_view_info& vi = infos[v];
+    vi.pixel_offset = pixels;
+    vi.width = w;
+    vi.height = h;
+    vi.tiles_x = tx;
+    vi.tiles_y = ty;
+    vi.tile_base = (uint32_t)tiles;
+    vi.splat_base = (uint32_t)splats;
+    vi.splat_count = sc.n;
+    vi.scene = in.scene;
+    max_sh = std::max(max_sh, d.sh ? sc.sh_degree : 0u);
+    splats += sc.n;
+    tiles += (uint64_t)tx * ty;
+    pixels += (uint64_t)w * h;
+    blocks += (sc.n + kPreBlock - 1) / kPreBlock;
+  }
+  if (splats > kMaxCapacity) return fail(c, GS3D_ERR_INVALID_ARG, "batch holds too many splats");
+  if (tiles >= (1ull << 31)) return fail(c, GS3D_ERR_INVALID_ARG, "batch holds too many tiles");
+  for (ViewDesc& d : vds) {
+    d.batch_splats = (uint32_t)splats;
+    d.batch_tiles = (uint32_t)tiles;
+  }
+
+  TRY(ensure_splat_buffers(c, (uint32_t)splats));
+  TRY(ensure(c, c->tile_offsets, (tiles + 1) * 4, "tile_offsets"));
+  TRY(ensure(c, c->tile_costs, std::max<uint64_t>(tiles, 1) * 4, "tile_costs"));
+  TRY(ensure(c, c->image, std::max<uint64_t>(pixels, 1) * 8, "splat_target"));
+  const size_t td = sort_capacity_round((uint32_t)std::max<uint64_t>(tiles, 1));
+  TRY(ensure(c, c->sched_keys_a, td * 4, "schedule keys"));
+  TRY(ensure(c, c->sched_keys_b, td * 4, "schedule keys"));
+  TRY(ensure(c, c->sched_order_a, td * 4, "schedule order"));
+  TRY(ensure(c, c->sched_order_b, td * 4, "schedule order"));
+  TRY(ensure(c, c->sched_status, sort_status_words((uint32_t)tiles, 4) * 4, "schedule status"));
+  TRY(ensure(c, c->d_views, (size_t)n_views * sizeof(ViewDesc), "view table"));
+  if (c->capacity < 1) TRY(ensure_key_capacity(c, 1));
+
+  if (n_views > c->upload_cap) {  // grow the pinned ring (idle stream first)
+    CK(cudaStreamSynchronize(c->stream), "upload ring resize");
+    if (c->h_upload) cudaFreeHost(c->h_upload);
+    c->h_upload = nullptr;
+    c->upload_cap = 0;
+    const size_t cap = std::max<size_t>(n_views, 64);
+    CK(cudaMallocHost(&c->h_upload, cap * kUploadSlots * sizeof(ViewDesc)), "pinned view ring");
+    c->upload_cap = cap;
+  }
+  const int slot = c->upload_slot;
+  c->upload_slot = (slot + 1) % kUploadSlots;
+  CK(cudaEventSynchronize(c->upload_ev[slot]), "view ring slot reuse");
+  ViewDesc* h = c->h_upload + (size_t)slot * c->upload_cap;
+  std::memcpy(h, vds.data(), n_views * sizeof(ViewDesc));
+  CK(cudaMemcpyAsync(c->d_views.p, h, n_views * sizeof(ViewDesc), cudaMemcpyHostToDevice,
+                     c->stream),
+     "upload view table");
+  CK(cudaEventRecord(c->upload_ev[slot], c->stream), "view ring event");
+
+  c->views.swap(vds);
+  c->info.swap(infos);
+  c->total_splats = (uint32_t)splats;
+  c->total_tiles = (uint32_t)tiles;
+  c->total_pixels = pixels;
+  c->total_blocks = (uint32_t)blocks;
+  c->max_sh = max_sh;
+  c->have_camera = true;
+  return GS3D_OK;
+}
+
+int require_frame(gs3d_ctx* c, const char* stage) {
+  if (!c->have_scene) return fail(c, GS3D_ERR_STATE, "%s: no splats set", stage);
+  if (!c->have_camera) return fail(c, GS3D_ERR_STATE, "%s: no camera set", stage);
+  return GS3D_OK;
+}
+
+int require_single(gs3d_ctx* c, const char* stage) {
+  TRY(require_frame(c, stage));
+  if (c->views.size() != 1)
+    return fail(c, GS3D_ERR_STATE, "%s: the stage entry points run one view (set_camera)", stage);
+  return GS3D_OK;
+}
+
+SortPlan tile_digit_plan(uint32_t num_tiles) {
+  const SortPlan full = make_sort_plan(num_tiles);
+  SortPlan tp{};
+  for (int p = 4; p < full.passes; ++p) {  // the tile-id digit places only
+    tp.word[tp.passes] = full.word[p];
+    tp.shift[tp.passes] = full.shift[p];
+    ++tp.passes;
+  }
+  return tp;
+}
+
+int raster_stage(gs3d_ctx* c, bool culled) {
+  StageScope t(c, GS3D_STAGE_RASTER);
+  const uint32_t* order = nullptr;
+  if (c->schedule != GS3D_SCHEDULE_ROW_MAJOR && c->total_tiles > 1) {
+    CK(launch_schedule(c->schedule, u32(c->tile_offsets), c->total_tiles,
+                       &dviews(c)->batch_tiles, u32(c->sched_keys_a), u32(c->sched_order_a), u32(c->sched_keys_b),
+                       u32(c->sched_order_b), u32(c->sched_status), ctrl_of(c), c->sm_count,
+                       c->stream),
+       "raster schedule");
+    order = u32(c->sched_order_a);
+  }
+  RasterArgs a{};
+  a.views = dviews(c);
+  a.n_views = (uint32_t)c->views.size();
+  a.num_tiles = c->total_tiles;
+  a.tile_w = c->tile_w;
+  a.tile_h = c->tile_h;
+  a.proj = static_cast<gs3d_projected_splat*>(c->proj.p);
+  a.tile_offsets = u32(c->tile_offsets);
+  a.values = u32(c->vals_a);
+  a.image = static_cast<uint2*>(c->image.p);
+  a.tile_costs = u32(c->tile_costs);
+  a.order = order;
+  a.queue_counter = &ctrl_of(c)->raster_queue;
+  a.culled = culled;
+  CK(cudaMemsetAsync(a.queue_counter, 0, sizeof(uint32_t), c->stream), "reset raster queue");
+  CK(launch_raster(a, c->sm_count, c->stream), "rasterize_tiles");
+  return GS3D_OK;
+}
+
+// Fused rebin over the current batch: depth digits sorted over splat-views,
+// refs emitted in depth order, tile digits sorted over refs.  For every view
+// the sorted keys, values, tile_offsets and image equal the stage-wise
+// sequence's.
+int fused_rebin(gs3d_ctx* c) {
+  TRY(require_frame(c, "rebin"));
+  Ctrl* k = ctrl_of(c);
+  const uint32_t nv = (uint32_t)c->views.size();
+  CK(cudaMemsetAsync(c->ctrl.p, 0, sizeof(Ctrl), c->stream), "reset control block");
+  {
+    StageScope t(c, GS3D_STAGE_PREPROCESS);
+    CK(launch_preprocess(dviews(c), nv, c->total_blocks, c->max_sh,
+                         static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->counts),
+                         u32(c->depth_keys_a), u32(c->depth_ids_a), &k->error, c->stream),
+       "preprocess");
+  }
+  {
+    StageScope t(c, GS3D_STAGE_DEPTH_SORT);
+    CK(launch_sort_depth_keys(&dviews(c)->batch_splats, c->total_splats, u32(c->depth_keys_a),
+                              u32(c->depth_ids_a), u32(c->depth_keys_b), u32(c->depth_ids_b),
+                              u32(c->depth_status), &k->sort_hist[0][0],
+                              &k->sort_part_counter[0], &k->error, c->sm_count, c->stream),
+       "depth sort");
+  }
+  c->scan_epoch = (c->scan_epoch % ((1u << 30) - 1)) + 1;
+  {
+    StageScope t(c, GS3D_STAGE_SCAN);
+    CK(launch_scan(u32(c->counts), u32(c->depth_ids_a), u32(c->sorted_offsets), c->total_splats,
+                   static_cast<unsigned long long*>(c->scan_status.p), &k->scan_tile_counter,
+                   c->scan_epoch, u32(c->ref_counter), &k->error, c->stream),
+       "prefix scan (depth order)");
+  }
+  const SortPlan tp = tile_digit_plan(c->total_tiles);
+  {
+    StageScope t(c, GS3D_STAGE_EMIT);
+    CK(launch_emit_sorted(dviews(c), nv, c->total_splats,
+                          static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->depth_ids_a),
+                          u32(c->sorted_offsets), u32(c->ref_counter), c->capacity,
+                          static_cast<uint2*>(c->keys_a.p), u32(c->vals_a), tp,
+                          &k->sort_hist[4][0], &k->error, c->stream),
+       "emit (depth order)");
+  }
+  {
+    StageScope t(c, GS3D_STAGE_SORT);
+    CK(launch_sort_tile_passes(tp, u32(c->ref_counter), c->capacity,
+                               static_cast<uint2*>(c->keys_a.p), u32(c->vals_a),
+                               static_cast<uint2*>(c->keys_b.p), u32(c->vals_b),
+                               u32(c->sort_status), &k->sort_hist[4][0], &k->sort_part_counter[4],
+                               &k->error, c->sm_count, c->stream),
+       "tile-digit sort");
+  }
+  if (tp.passes % 2) {
+    std::swap(c->keys_a, c->keys_b);
+    std::swap(c->vals_a, c->vals_b);
+  }
+  {
+    StageScope t(c, GS3D_STAGE_IDENTIFY);
+    CK(launch_identify(static_cast<uint2*>(c->keys_a.p), u32(c->ref_counter), c->capacity,
+                       c->total_tiles, u32(c->tile_offsets), &k->error, c->sm_count, c->stream),
+       "identify_tile_ranges");
+  }
+  return raster_stage(c, true);
+}
+
 }  // namespace
 
 extern "C" {
 
 int gs3d_abi_version(void) { return GS3D_ABI_VERSION; }
 
-const char* gs3d_last_error(const gs3d_ctx* c) {
-  return c ? c->err.c_str() : "null context";
-}
+const char* gs3d_last_error(const gs3d_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
 int gs3d_create(gs3d_ctx** out, const gs3d_config* cfg) {
   if (!out) return GS3D_ERR_INVALID_ARG;
@@ -300,15 +582,13 @@ int gs3d_create(gs3d_ctx** out, const gs3d_config* cfg) {
   }
   probe_kernel<<<1, 1, 0, c->stream>>>(nullptr);
   if (cudaGetLastError() != cudaSuccess) return bail(GS3D_ERR_NO_DEVICE);
-  if (ensure(c, c->frame, sizeof(FrameUniforms), "frame uniforms") != GS3D_OK ||
-      ensure(c, c->ctrl, sizeof(Ctrl), "control block") != GS3D_OK ||
+  c->scenes.resize(1);
+  if (ensure(c, c->ctrl, sizeof(Ctrl), "control block") != GS3D_OK ||
       ensure(c, c->ref_counter, 16, "ref_counter") != GS3D_OK)
     return bail(GS3D_ERR_OOM);
-  if (cudaMallocHost(&c->h_frames, sizeof(FrameUniforms) * kFrameSlots) != cudaSuccess ||
-      cudaMallocHost(&c->h_word, 64) != cudaSuccess)
-    return bail(GS3D_ERR_OOM);
-  for (int i = 0; i < kFrameSlots; ++i)
-    if (cudaEventCreateWithFlags(&c->frame_ev[i], cudaEventDisableTiming) != cudaSuccess)
+  if (cudaMallocHost(&c->h_word, 64) != cudaSuccess) return bail(GS3D_ERR_OOM);
+  for (int i = 0; i < kUploadSlots; ++i)
+    if (cudaEventCreateWithFlags(&c->upload_ev[i], cudaEventDisableTiming) != cudaSuccess)
       return bail(GS3D_ERR_CUDA);
   if (cudaMemsetAsync(c->ctrl.p, 0, sizeof(Ctrl), c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->ref_counter.p, 0, 16, c->stream) != cudaSuccess ||
@@ -322,18 +602,25 @@ int gs3d_destroy(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  DevBuf* bufs[] = {&c->pos,        &c->scale,        &c->rot,         &c->color,
-                    &c->sh,         &c->proj,         &c->counts,      &c->offsets,
-                    &c->ref_counter, &c->keys_a,      &c->vals_a,      &c->keys_b,
-                    &c->vals_b,     &c->scan_status,  &c->sort_status, &c->frame,
-                    &c->tile_offsets, &c->image,      &c->tile_costs,  &c->ctrl,
-                    &c->depth_keys_a, &c->depth_ids_a, &c->depth_keys_b, &c->depth_ids_b,
-                    &c->sorted_offsets, &c->depth_status};
+  for (SceneBufs& s : c->scenes) {
+    release(s.pos);
+    release(s.scale);
+    release(s.rot);
+    release(s.color);
+    release(s.sh);
+  }
+  DevBuf* bufs[] = {&c->proj,          &c->counts,        &c->offsets,       &c->ref_counter,
+                    &c->keys_a,        &c->vals_a,        &c->keys_b,        &c->vals_b,
+                    &c->scan_status,   &c->sort_status,   &c->depth_keys_a,  &c->depth_ids_a,
+                    &c->depth_keys_b,  &c->depth_ids_b,   &c->sorted_offsets, &c->depth_status,
+                    &c->tile_offsets,  &c->image,         &c->tile_costs,    &c->sched_keys_a,
+                    &c->sched_keys_b,  &c->sched_order_a, &c->sched_order_b, &c->sched_status,
+                    &c->d_views,       &c->ctrl};
   for (DevBuf* b : bufs) release(*b);
-  for (int i = 0; i < kFrameSlots; ++i)
-    if (c->frame_ev[i]) cudaEventDestroy(c->frame_ev[i]);
+  for (int i = 0; i < kUploadSlots; ++i)
+    if (c->upload_ev[i]) cudaEventDestroy(c->upload_ev[i]);
   for (auto& e : c->ev_pool) cudaEventDestroy(e);
-  if (c->h_frames) cudaFreeHost(c->h_frames);
+  if (c->h_upload) cudaFreeHost(c->h_upload);
   if (c->h_word) cudaFreeHost(c->h_word);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -344,48 +631,40 @@ int gs3d_set_splats(gs3d_ctx* c, uint32_t n, const float* positions, const float
                     const float* rotations, const float* colors, const float* sh_rest,
                     uint32_t sh_degree, int memory) {
   if (!c) return GS3D_ERR_INVALID_ARG;
-  if (memory != 0 && memory != 1) return fail(c, GS3D_ERR_INVALID_ARG, "memory must be 0 or 1");
-  if (sh_degree > 3) return fail(c, GS3D_ERR_INVALID_ARG, "sh_degree %u > 3", sh_degree);
-  if (n > 0 && (!positions || !scales || !rotations || !colors))
-    return fail(c, GS3D_ERR_INVALID_ARG, "null splat array");
-  if (n > 0 && sh_degree > 0 && !sh_rest)
-    return fail(c, GS3D_ERR_INVALID_ARG, "sh_degree %u needs sh_rest", sh_degree);
-  if (n > (1u << 30)) return fail(c, GS3D_ERR_INVALID_ARG, "too many splats (%u)", n);
-  TRY(set_device(c));
-  const size_t v4 = (size_t)n * 16;
-  const uint32_t kc = 3u * ((sh_degree + 1) * (sh_degree + 1) - 1);
-  TRY(ensure(c, c->pos, v4, "splat_positions"));
-  TRY(ensure(c, c->scale, v4, "splat_scales"));
-  TRY(ensure(c, c->rot, v4, "splat_rotations"));
-  TRY(ensure(c, c->color, v4, "splat_colors"));
-  if (kc) TRY(ensure(c, c->sh, (size_t)n * kc * sizeof(float), "splat_sh_rest"));
-  const cudaMemcpyKind kind = memory ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  if (n) {
-    CK(cudaMemcpyAsync(c->pos.p, positions, v4, kind, c->stream), "upload positions");
-    CK(cudaMemcpyAsync(c->scale.p, scales, v4, kind, c->stream), "upload scales");
-    CK(cudaMemcpyAsync(c->rot.p, rotations, v4, kind, c->stream), "upload rotations");
-    CK(cudaMemcpyAsync(c->color.p, colors, v4, kind, c->stream), "upload colors");
-    if (kc)
-      CK(cudaMemcpyAsync(c->sh.p, sh_rest, (size_t)n * kc * sizeof(float), kind, c->stream),
-         "upload sh_rest");
-  }
+  TRY(upload_scene(c, c->scenes[0], n, positions, scales, rotations, colors, sh_rest, sh_degree,
+                   memory));
   // resizeBinningBuffers (GaussianSplatRenderer.ts:209-227)
-  TRY(ensure(c, c->proj, (size_t)n * sizeof(gs3d_projected_splat), "projected_splats"));
-  TRY(ensure(c, c->counts, (size_t)n * 4, "splat_ref_counts"));
-  TRY(ensure(c, c->offsets, ((size_t)n + 1) * 4, "splat_ref_offsets"));
-  TRY(ensure(c, c->scan_status, scan_status_words(n) * 8, "scan look-back status"));
-  TRY(ensure(c, c->depth_keys_a, (size_t)n * 4, "depth keys"));
-  TRY(ensure(c, c->depth_keys_b, (size_t)n * 4, "depth keys"));
-  TRY(ensure(c, c->depth_ids_a, (size_t)n * 4, "depth ids"));
-  TRY(ensure(c, c->depth_ids_b, (size_t)n * 4, "depth ids"));
-  TRY(ensure(c, c->sorted_offsets, ((size_t)n + 1) * 4, "depth-ordered offsets"));
-  TRY(ensure(c, c->depth_status, sort_status_words(n, 4) * 4, "depth sort status"));
+  TRY(ensure_splat_buffers(c, n));
   TRY(ensure_key_capacity(
       c, std::min<uint64_t>((uint64_t)std::max<uint32_t>(n, 1) * c->max_tiles_per_splat,
                             kMaxCapacity)));
-  CK(cudaStreamSynchronize(c->stream), "splat upload");
-  c->n = n;
-  c->sh_degree = sh_degree;
+  c->have_scene = true;
+  c->have_camera = false;  // the view table refers to the scene's size
+  return GS3D_OK;
+}
+
+int gs3d_add_scene(gs3d_ctx* c, uint32_t n, const float* positions, const float* scales,
+                   const float* rotations, const float* colors, const float* sh_rest,
+                   uint32_t sh_degree, int memory, uint32_t* out_scene) {
+  if (!c || !out_scene) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
+  SceneBufs sc;
+  const int rc = upload_scene(c, sc, n, positions, scales, rotations, colors, sh_rest, sh_degree,
+                              memory);
+  if (rc != GS3D_OK) {
+    release(sc.pos);
+    release(sc.scale);
+    release(sc.rot);
+    release(sc.color);
+    release(sc.sh);
+    return rc;
+  }
+  if (!c->have_scene) {  // the first scene also fills slot 0
+    c->scenes[0] = sc;
+    *out_scene = 0;
+  } else {
+    c->scenes.push_back(sc);
+    *out_scene = (uint32_t)c->scenes.size() - 1;
+  }
   c->have_scene = true;
   return GS3D_OK;
 }
@@ -407,172 +686,70 @@ int gs3d_set_tile_size(gs3d_ctx* c, uint32_t tx, uint32_t ty, uint32_t* out_x, u
 
 int gs3d_set_camera(gs3d_ctx* c, const gs3d_camera* cam, uint32_t width, uint32_t height) {
   if (!c || !cam) return fail(c, GS3D_ERR_INVALID_ARG, "null camera");
+  if (!c->have_scene) return fail(c, GS3D_ERR_STATE, "set_camera: no splats set");
   TRY(set_device(c));
-  width = std::max<uint32_t>(1, width);  // GaussianSplatRenderer.ts:1040-1041
-  height = std::max<uint32_t>(1, height);
-  const uint32_t tx = (width + c->tile_w - 1) / c->tile_w;  // :1042-1043
-  const uint32_t ty = (height + c->tile_h - 1) / c->tile_h;
-  const uint64_t tiles = (uint64_t)tx * ty;
-  if (tiles >= (1ull << 31)) return fail(c, GS3D_ERR_INVALID_ARG, "viewport too large");
-  TRY(ensure(c, c->tile_offsets, (tiles + 1) * 4, "tile_offsets"));
-  TRY(ensure(c, c->tile_costs, tiles * 4, "tile_costs"));
-  TRY(ensure(c, c->image, (size_t)width * height * 8, "splat_target"));
-  c->W = width;
-  c->H = height;
-  c->tiles_x = tx;
-  c->tiles_y = ty;
-
-  const int slot = c->frame_slot;
-  c->frame_slot = (slot + 1) % kFrameSlots;
-  CK(cudaEventSynchronize(c->frame_ev[slot]), "frame slot reuse");
-  FrameUniforms& f = c->h_frames[slot];
-  std::memset(&f, 0, sizeof(f));
-  f.cam = *cam;
-  f.tile_count[0] = tx;
-  f.tile_count[1] = ty;
-  f.splat_count = c->n;
-  f.num_tiles = (uint32_t)tiles;
-  f.inv_tile[0] = (float)(1.0 / c->tile_w);  // :1127-1128, f64 division stored as f32
-  f.inv_tile[1] = (float)(1.0 / c->tile_h);
-  f.viewport[0] = width;
-  f.viewport[1] = height;
-  f.tile_size[0] = c->tile_w;
-  f.tile_size[1] = c->tile_h;
-  CK(cudaMemcpyAsync(c->frame.p, &f, sizeof(f), cudaMemcpyHostToDevice, c->stream),
-     "upload frame uniforms");
-  CK(cudaEventRecord(c->frame_ev[slot], c->stream), "frame event");
-  c->have_camera = true;
-  return GS3D_OK;
+  gs3d_view v{};
+  v.camera = *cam;
+  v.scene = 0;
+  v.width = width;
+  v.height = height;
+  return set_views(c, &v, 1);
 }
 
 int gs3d_preprocess(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
-  TRY(require_frame(c, "preprocess"));
+  TRY(require_single(c, "preprocess"));
   TRY(set_device(c));
   // start of a frame: counters, histograms and the error latch
   CK(cudaMemsetAsync(c->ctrl.p, 0, sizeof(Ctrl), c->stream), "reset control block");
   StageScope t(c, GS3D_STAGE_PREPROCESS);
-  CK(launch_preprocess(static_cast<FrameUniforms*>(c->frame.p), c->n,
-                       static_cast<float4*>(c->pos.p), static_cast<float4*>(c->scale.p),
-                       static_cast<float4*>(c->rot.p), static_cast<float4*>(c->color.p),
-                       c->sh_degree ? static_cast<float*>(c->sh.p) : nullptr, c->sh_degree,
-                       static_cast<gs3d_projected_splat*>(c->proj.p),
-                       static_cast<uint32_t*>(c->counts.p), nullptr, nullptr,
-                       &ctrl_of(c)->error, c->stream),
+  CK(launch_preprocess(dviews(c), 1, c->total_blocks, c->max_sh,
+                       static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->counts), nullptr,
+                       nullptr, &ctrl_of(c)->error, c->stream),
      "preprocess");
-  return GS3D_OK;
-}
-
-// Fused rebin (the default): depth digits sorted over splats, refs emitted in
-// depth order, tile digits sorted over refs.  Same sorted keys, values,
-// tile_offsets and image as the stage-wise sequence.
-static int fused_rebin(gs3d_ctx* c) {
-  TRY(require_frame(c, "rebin"));
-  Ctrl* k = ctrl_of(c);
-  FrameUniforms* fu = static_cast<FrameUniforms*>(c->frame.p);
-  CK(cudaMemsetAsync(c->ctrl.p, 0, sizeof(Ctrl), c->stream), "reset control block");
-  auto u32 = [](DevBuf& b) { return static_cast<uint32_t*>(b.p); };
-  {
-  StageScope t(c, GS3D_STAGE_PREPROCESS);
-  CK(launch_preprocess(fu, c->n, static_cast<float4*>(c->pos.p), static_cast<float4*>(c->scale.p),
-                       static_cast<float4*>(c->rot.p), static_cast<float4*>(c->color.p),
-                       c->sh_degree ? static_cast<float*>(c->sh.p) : nullptr, c->sh_degree,
-                       static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->counts),
-                       u32(c->depth_keys_a), u32(c->depth_ids_a), &k->error, c->stream),
-     "preprocess");
-  }
-  {
-  StageScope t(c, GS3D_STAGE_DEPTH_SORT);
-  CK(launch_sort_depth_keys(&fu->splat_count, c->n, u32(c->depth_keys_a), u32(c->depth_ids_a),
-                            u32(c->depth_keys_b), u32(c->depth_ids_b), u32(c->depth_status),
-                            &k->sort_hist[0][0], &k->sort_part_counter[0], &k->error,
-                            c->sm_count, c->stream),
-     "depth sort");
-  }
-  c->scan_epoch = (c->scan_epoch % ((1u << 30) - 1)) + 1;
-  {
-  StageScope t(c, GS3D_STAGE_SCAN);
-  CK(launch_scan(u32(c->counts), u32(c->depth_ids_a), u32(c->sorted_offsets), c->n,
-                 static_cast<unsigned long long*>(c->scan_status.p), &k->scan_tile_counter,
-                 c->scan_epoch, u32(c->ref_counter), &k->error, c->stream),
-     "prefix scan (depth order)");
-  }
-  const SortPlan full = make_sort_plan(c->tiles_x * c->tiles_y);
-  SortPlan tp{};
-  for (int p = 4; p < full.passes; ++p) {  // the tile-id digit places only
-    tp.word[tp.passes] = full.word[p];
-    tp.shift[tp.passes] = full.shift[p];
-    ++tp.passes;
-  }
-  {
-  StageScope t(c, GS3D_STAGE_EMIT);
-  CK(launch_emit_sorted(fu, c->n, static_cast<gs3d_projected_splat*>(c->proj.p),
-                        u32(c->depth_ids_a), u32(c->sorted_offsets), u32(c->ref_counter),
-                        c->capacity, static_cast<uint2*>(c->keys_a.p), u32(c->vals_a), tp,
-                        &k->sort_hist[4][0], &k->error, c->stream),
-     "emit (depth order)");
-  }
-  {
-  StageScope t(c, GS3D_STAGE_SORT);
-  CK(launch_sort_tile_passes(tp, u32(c->ref_counter), c->capacity,
-                             static_cast<uint2*>(c->keys_a.p), u32(c->vals_a),
-                             static_cast<uint2*>(c->keys_b.p), u32(c->vals_b),
-                             u32(c->sort_status), &k->sort_hist[4][0], &k->sort_part_counter[4],
-                             &k->error, c->sm_count, c->stream),
-     "tile-digit sort");
-  }
-  if (tp.passes % 2) {
-    std::swap(c->keys_a, c->keys_b);
-    std::swap(c->vals_a, c->vals_b);
-  }
-  TRY(gs3d_identify_tile_ranges(c));
-  TRY(gs3d_rasterize_tiles(c));
   return GS3D_OK;
 }
 
 int gs3d_prefix_scan(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
-  TRY(require_frame(c, "prefix_scan"));
+  TRY(require_single(c, "prefix_scan"));
   TRY(set_device(c));
   CK(cudaMemsetAsync(&ctrl_of(c)->scan_tile_counter, 0, sizeof(uint32_t), c->stream),
      "reset scan ticket");
   c->scan_epoch = (c->scan_epoch % ((1u << 30) - 1)) + 1;  // 1 .. 2^30-1, never 0
   StageScope t(c, GS3D_STAGE_SCAN);
-  CK(launch_scan(static_cast<uint32_t*>(c->counts.p), nullptr,
-                 static_cast<uint32_t*>(c->offsets.p), c->n,
+  CK(launch_scan(u32(c->counts), nullptr, u32(c->offsets), c->total_splats,
                  static_cast<unsigned long long*>(c->scan_status.p),
-                 &ctrl_of(c)->scan_tile_counter, c->scan_epoch,
-                 static_cast<uint32_t*>(c->ref_counter.p), &ctrl_of(c)->error, c->stream),
+                 &ctrl_of(c)->scan_tile_counter, c->scan_epoch, u32(c->ref_counter),
+                 &ctrl_of(c)->error, c->stream),
      "prefix scan");
   return GS3D_OK;
 }
 
 int gs3d_emit_tile_refs(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
-  TRY(require_frame(c, "emit_tile_refs"));
+  TRY(require_single(c, "emit_tile_refs"));
   TRY(set_device(c));
   StageScope t(c, GS3D_STAGE_EMIT);
-  CK(launch_emit(static_cast<FrameUniforms*>(c->frame.p), c->n,
-                 static_cast<gs3d_projected_splat*>(c->proj.p),
-                 static_cast<uint32_t*>(c->offsets.p), static_cast<uint32_t*>(c->ref_counter.p),
-                 c->capacity, static_cast<uint2*>(c->keys_a.p),
-                 static_cast<uint32_t*>(c->vals_a.p), &ctrl_of(c)->error, c->stream),
+  CK(launch_emit(&dviews(c)->f, c->total_splats, static_cast<gs3d_projected_splat*>(c->proj.p),
+                 u32(c->offsets), u32(c->ref_counter), c->capacity,
+                 static_cast<uint2*>(c->keys_a.p), u32(c->vals_a), &ctrl_of(c)->error,
+                 c->stream),
      "emit_tile_refs");
   return GS3D_OK;
 }
 
 int gs3d_radix_sort(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
-  TRY(require_frame(c, "radix_sort"));
+  TRY(require_single(c, "radix_sort"));
   TRY(set_device(c));
-  const SortPlan plan = make_sort_plan(c->tiles_x * c->tiles_y);
+  const SortPlan plan = make_sort_plan(c->total_tiles);
   {
-  StageScope t(c, GS3D_STAGE_SORT);
-  CK(launch_sort(plan, static_cast<uint32_t*>(c->ref_counter.p), c->capacity,
-                 static_cast<uint2*>(c->keys_a.p), static_cast<uint32_t*>(c->vals_a.p),
-                 static_cast<uint2*>(c->keys_b.p), static_cast<uint32_t*>(c->vals_b.p),
-                 static_cast<uint32_t*>(c->sort_status.p), ctrl_of(c), c->sm_count, c->stream),
-     "radix sort");
+    StageScope t(c, GS3D_STAGE_SORT);
+    CK(launch_sort(plan, u32(c->ref_counter), c->capacity, static_cast<uint2*>(c->keys_a.p),
+                   u32(c->vals_a), static_cast<uint2*>(c->keys_b.p), u32(c->vals_b),
+                   u32(c->sort_status), ctrl_of(c), c->sm_count, c->stream),
+       "radix sort");
   }
   if (plan.passes % 2) {  // sorted data ended in the B buffers: rename
     std::swap(c->keys_a, c->keys_b);
@@ -586,9 +763,8 @@ int gs3d_identify_tile_ranges(gs3d_ctx* c) {
   TRY(require_frame(c, "identify_tile_ranges"));
   TRY(set_device(c));
   StageScope t(c, GS3D_STAGE_IDENTIFY);
-  CK(launch_identify(static_cast<uint2*>(c->keys_a.p), static_cast<uint32_t*>(c->ref_counter.p),
-                     c->capacity, c->tiles_x * c->tiles_y,
-                     static_cast<uint32_t*>(c->tile_offsets.p), &ctrl_of(c)->error, c->sm_count,
+  CK(launch_identify(static_cast<uint2*>(c->keys_a.p), u32(c->ref_counter), c->capacity,
+                     c->total_tiles, u32(c->tile_offsets), &ctrl_of(c)->error, c->sm_count,
                      c->stream),
      "identify_tile_ranges");
   return GS3D_OK;
@@ -598,14 +774,7 @@ int gs3d_rasterize_tiles(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
   TRY(require_frame(c, "rasterize_tiles"));
   TRY(set_device(c));
-  StageScope t(c, GS3D_STAGE_RASTER);
-  CK(launch_raster(static_cast<FrameUniforms*>(c->frame.p), c->tiles_x, c->tiles_y, c->tile_w,
-                   c->tile_h, static_cast<gs3d_projected_splat*>(c->proj.p),
-                   static_cast<uint32_t*>(c->tile_offsets.p),
-                   static_cast<uint32_t*>(c->vals_a.p), static_cast<uint2*>(c->image.p),
-                   static_cast<uint32_t*>(c->tile_costs.p), c->stream),
-     "rasterize_tiles");
-  return GS3D_OK;
+  return raster_stage(c, /*culled=*/!(c->flags & GS3D_FLAG_STAGEWISE_REBIN));
 }
 
 int gs3d_rebin(gs3d_ctx* c, const gs3d_camera* cam, uint32_t width, uint32_t height) {
@@ -619,6 +788,31 @@ int gs3d_rebin(gs3d_ctx* c, const gs3d_camera* cam, uint32_t width, uint32_t hei
   TRY(gs3d_radix_sort(c));
   TRY(gs3d_identify_tile_ranges(c));
   TRY(gs3d_rasterize_tiles(c));
+  return GS3D_OK;
+}
+
+int gs3d_rebin_batch(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  if (!c->have_scene) return fail(c, GS3D_ERR_STATE, "rebin_batch: no scene");
+  TRY(set_device(c));
+  TRY(set_views(c, views, n_views));
+  return fused_rebin(c);
+}
+
+int gs3d_get_view_info(gs3d_ctx* c, uint32_t view, gs3d_view_info* out) {
+  if (!c || !out) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
+  if (view >= c->info.size())
+    return fail(c, GS3D_ERR_INVALID_ARG, "view %u out of range (%zu views)", view,
+                c->info.size());
+  *out = c->info[view];
+  return GS3D_OK;
+}
+
+int gs3d_set_schedule(gs3d_ctx* c, uint32_t schedule) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  if (schedule > GS3D_SCHEDULE_KEY_COUNT)
+    return fail(c, GS3D_ERR_INVALID_ARG, "unknown schedule %u", schedule);
+  c->schedule = schedule;
   return GS3D_OK;
 }
 
@@ -650,12 +844,13 @@ int gs3d_synchronize(gs3d_ctx* c) {
 }
 
 static DevBuf* named(gs3d_ctx* c, gs3d_buffer which) {
+  SceneBufs& s0 = c->scenes[0];
   switch (which) {
-    case GS3D_BUF_SPLAT_POSITIONS: return &c->pos;
-    case GS3D_BUF_SPLAT_SCALES: return &c->scale;
-    case GS3D_BUF_SPLAT_ROTATIONS: return &c->rot;
-    case GS3D_BUF_SPLAT_COLORS: return &c->color;
-    case GS3D_BUF_SPLAT_SH_REST: return &c->sh;
+    case GS3D_BUF_SPLAT_POSITIONS: return &s0.pos;
+    case GS3D_BUF_SPLAT_SCALES: return &s0.scale;
+    case GS3D_BUF_SPLAT_ROTATIONS: return &s0.rot;
+    case GS3D_BUF_SPLAT_COLORS: return &s0.color;
+    case GS3D_BUF_SPLAT_SH_REST: return &s0.sh;
     case GS3D_BUF_PROJECTED_SPLATS: return &c->proj;
     case GS3D_BUF_SPLAT_REF_COUNTS: return &c->counts;
     case GS3D_BUF_SPLAT_REF_OFFSETS: return &c->offsets;
@@ -730,7 +925,7 @@ int gs3d_ref_count(gs3d_ctx* c, uint32_t* out) {
 int gs3d_read_tile_counts(gs3d_ctx* c, uint32_t* counts, size_t n) {
   if (!c || !counts) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
   if (!c->have_camera) return fail(c, GS3D_ERR_STATE, "no frame");
-  const size_t tiles = (size_t)c->tiles_x * c->tiles_y;
+  const size_t tiles = c->total_tiles;
   if (n < tiles) return fail(c, GS3D_ERR_INVALID_ARG, "need room for %zu tiles", tiles);
   uint32_t* off = new (std::nothrow) uint32_t[tiles + 1];
   if (!off) return fail(c, GS3D_ERR_OOM, "host allocation");

@@ -79,14 +79,17 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// Fused-rebin emit: block b owns depth-sorted positions [256b, 256b+256); the
-// splat at position i is sorted_ids[i] and its refs start at
-// sorted_offsets[i].  Besides the keys/values it accumulates the 256-bin
-// histograms of the tile-id digit places that the following radix passes
-// sort, so those passes need no separate histogram read.
+// Fused-rebin emit over a batch: block b owns depth-sorted positions
+// [256b, 256b+256); the splat-view at position i is g = sorted_ids[i], it
+// belongs to the view v whose range holds g, and its refs start at
+// sorted_offsets[i].  Keys carry global tile ids (view tile base + local
+// tile) so the later tile-digit passes also separate the views; values carry
+// g.  Besides the keys/values the kernel accumulates the 256-bin histograms
+// of the tile-id digit places those passes sort, so they need no separate
+// histogram read.
 template <int TP>
 __global__ void __launch_bounds__(kThreads)
-    emit_sorted_kernel(const FrameUniforms* __restrict__ fu, uint32_t n,
+    emit_sorted_kernel(const ViewDesc* __restrict__ views, uint32_t n_views, uint32_t n,
                        const gs3d_projected_splat* __restrict__ proj,
                        const uint32_t* __restrict__ sorted_ids,
                        const uint32_t* __restrict__ sorted_offsets,
@@ -95,7 +98,7 @@ __global__ void __launch_bounds__(kThreads)
                        uint32_t* __restrict__ g_hist, uint32_t* __restrict__ err) {
   __shared__ uint32_t s_off[kThreads + 1];
   __shared__ uint32_t s_tminx[kThreads], s_tminy[kThreads], s_w[kThreads], s_cnt[kThreads];
-  __shared__ uint32_t s_lo[kThreads], s_id[kThreads];
+  __shared__ uint32_t s_lo[kThreads], s_id[kThreads], s_tx[kThreads], s_tb[kThreads];
   __shared__ uint32_t s_hist[TP > 0 ? TP : 1][kRadixBins];
 
   const uint32_t total = *ref_counter;
@@ -106,13 +109,14 @@ __global__ void __launch_bounds__(kThreads)
   for (int k = threadIdx.x; k < TP * kRadixBins; k += kThreads) (&s_hist[0][0])[k] = 0u;
   const uint32_t first = blockIdx.x * kThreads;
   const uint32_t i = first + threadIdx.x;
-  const uint32_t tiles_x = __ldg(&fu->tile_count[0]);
   if (i < n) {
     const uint32_t id = __ldg(sorted_ids + i);
     const float4 r0 = __ldg(reinterpret_cast<const float4*>(proj + id));
     const uint32_t valid = __ldg(&proj[id].valid);
     const uint4 r3 = __ldg(reinterpret_cast<const uint4*>(proj + id) + 3);
     const uint32_t w = r3.z - r3.x + 1u, h = r3.w - r3.y + 1u;
+    const uint32_t v =
+        find_view(n_views, id, [&](uint32_t k) { return __ldg(&views[k].splat_base); });
     s_off[threadIdx.x] = __ldg(sorted_offsets + i);
     s_tminx[threadIdx.x] = r3.x;
     s_tminy[threadIdx.x] = r3.y;
@@ -120,6 +124,8 @@ __global__ void __launch_bounds__(kThreads)
     s_cnt[threadIdx.x] = valid ? w * h : 0u;
     s_lo[threadIdx.x] = __float_as_uint(-r0.z);
     s_id[threadIdx.x] = id;
+    s_tx[threadIdx.x] = __ldg(&views[v].f.tile_count[0]);
+    s_tb[threadIdx.x] = __ldg(&views[v].f.tile_base);
   }
   const uint32_t last = min(n, first + kThreads);
   if (threadIdx.x == 0) s_off[last - first] = __ldg(sorted_offsets + last);
@@ -145,7 +151,7 @@ __global__ void __launch_bounds__(kThreads)
       const uint32_t k = j - s_off[lo];
       if (k < s_cnt[lo]) {
         const uint32_t w = s_w[lo];
-        tile = (s_tminy[lo] + k / w) * tiles_x + s_tminx[lo] + k % w;
+        tile = s_tb[lo] + (s_tminy[lo] + k / w) * s_tx[lo] + s_tminx[lo] + k % w;
         keys[j] = make_uint2(tile, s_lo[lo]);
         values[j] = s_id[lo];
       } else {
@@ -164,7 +170,7 @@ __global__ void __launch_bounds__(kThreads)
 
 }  // namespace
 
-cudaError_t launch_emit_sorted(const FrameUniforms* d_frame, uint32_t n,
+cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t n,
                                const gs3d_projected_splat* proj, const uint32_t* sorted_ids,
                                const uint32_t* sorted_offsets, const uint32_t* ref_counter,
                                uint32_t capacity, uint2* keys, uint32_t* values,
@@ -175,11 +181,11 @@ cudaError_t launch_emit_sorted(const FrameUniforms* d_frame, uint32_t n,
   int4 sh = make_int4(0, 0, 0, 0);
   int* shp = &sh.x;
   for (int p = 0; p < tile_plan.passes && p < 4; ++p) shp[p] = tile_plan.shift[p];
-#define GS3D_EMIT_CASE(TP)                                                                   \
-  case TP:                                                                                  \
-    emit_sorted_kernel<TP><<<blocks, kThreads, 0, s>>>(d_frame, n, proj, sorted_ids,         \
-                                                       sorted_offsets, ref_counter, capacity, \
-                                                       keys, values, sh, g_hist, err);        \
+#define GS3D_EMIT_CASE(TP)                                                                     \
+  case TP:                                                                                    \
+    emit_sorted_kernel<TP><<<blocks, kThreads, 0, s>>>(views, n_views, n, proj, sorted_ids,    \
+                                                       sorted_offsets, ref_counter, capacity,  \
+                                                       keys, values, sh, g_hist, err);         \
     break;
   switch (tile_plan.passes) {
     GS3D_EMIT_CASE(0)

@@ -27,6 +27,39 @@ struct FrameUniforms {
 };
 static_assert(sizeof(FrameUniforms) % 16 == 0, "FrameUniforms is copied as 16-byte words");
 
+// One view of a batched rebin.  A single-view rebin is a batch of one.
+// Splat-views of all views are concatenated (view v owns global indices
+// [splat_base, splat_base + f.splat_count)), and so are tiles (global tile
+// id = f.tile_base + ty * tiles_x + tx) and images (pixel_base).
+struct ViewDesc {
+  FrameUniforms f;
+  const float4* pos;
+  const float4* scale;
+  const float4* rot;
+  const float4* color;
+  const float* sh;
+  uint32_t sh_degree;
+  uint32_t splat_base;
+  uint32_t block_base;  // first preprocess block of this view
+  uint32_t batch_splats;  // splat-views in the whole batch (same in every view)
+  uint64_t pixel_base;  // first pixel of this view's image in the batch target
+  uint32_t batch_tiles;   // tiles in the whole batch (same in every view)
+  uint32_t pad1;
+  uint64_t pad2;
+};
+static_assert(sizeof(ViewDesc) % 16 == 0, "ViewDesc is copied as 16-byte words");
+
+// Largest v with key(v) <= x over a non-decreasing per-view field.
+template <typename F>
+__device__ __forceinline__ uint32_t find_view(uint32_t n_views, uint32_t x, F key) {
+  uint32_t lo = 0, hi = n_views;  // key(lo) <= x < key(hi) (key(n_views) = inf)
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (key(mid) <= x) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
 // Device error latch bits (read and cleared by gs3d_synchronize).
 enum : uint32_t {
   DEVERR_CAPACITY = 1u,  // live ref count exceeded key capacity: nothing written
@@ -42,8 +75,11 @@ struct Ctrl {
   uint32_t error;
   uint32_t scan_tile_counter;
   uint32_t sort_part_counter[kMaxSortPasses];
-  uint32_t pad[6];
+  uint32_t raster_queue;
+  uint32_t sched_counter[2];
+  uint32_t pad[3];
   uint32_t sort_hist[kMaxSortPasses][kRadixBins];  // global digit histograms
+  uint32_t sched_hist[2][kRadixBins];
 };
 
 // Bounded spins: a device wait gives up after this many polls (with
@@ -160,16 +196,19 @@ struct SortPlan {
 };
 SortPlan make_sort_plan(uint32_t num_tiles);
 
-cudaError_t launch_preprocess(const FrameUniforms* d_frame, uint32_t n, const float4* pos,
-                              const float4* scale, const float4* rot, const float4* color,
-                              const float* sh_rest, uint32_t sh_degree,
-                              gs3d_projected_splat* out, uint32_t* counts, uint32_t* depth_keys,
-                              uint32_t* depth_ids, uint32_t* err, cudaStream_t s);
+// Projects every splat-view of the batch (total_blocks = sum of
+// ceil(splat_count / 256) over views; max_sh_degree bounds the views' SH
+// degrees and sizes the shared-memory staging).
+cudaError_t launch_preprocess(const ViewDesc* views, uint32_t n_views, uint32_t total_blocks,
+                              uint32_t max_sh_degree, gs3d_projected_splat* out, uint32_t* counts,
+                              uint32_t* depth_keys, uint32_t* depth_ids, uint32_t* err,
+                              cudaStream_t s);
 // Exclusive scan of counts[gather[i]] (counts[i] when gather is null).
 cudaError_t launch_scan(const uint32_t* counts, const uint32_t* gather, uint32_t* offsets,
                         uint32_t n, unsigned long long* status, uint32_t* tile_counter,
                         uint32_t epoch, uint32_t* total_out, uint32_t* err, cudaStream_t s);
 size_t scan_status_words(uint32_t n);
+// Emit in splat order (the reference's emit_tile_refs, one view).
 cudaError_t launch_emit(const FrameUniforms* d_frame, uint32_t n,
                         const gs3d_projected_splat* proj, const uint32_t* offsets,
                         const uint32_t* ref_counter, uint32_t capacity, uint2* keys,
@@ -178,19 +217,38 @@ cudaError_t launch_sort(const SortPlan& plan, const uint32_t* ref_counter, uint3
                         uint2* keys_a, uint32_t* vals_a, uint2* keys_b, uint32_t* vals_b,
                         uint32_t* status, Ctrl* ctrl, int sm_count, cudaStream_t s);
 size_t sort_status_words(uint32_t capacity, int passes);
+// Key/value buffers handed to the sort must hold this many entries: passes
+// always fetch whole 4096-key partitions (entries past the live count are
+// read and ignored).
+uint32_t sort_capacity_round(uint32_t capacity);
 // Tile-id passes of the fused rebin: histograms already in g_hist[p][256].
 cudaError_t launch_sort_tile_passes(const SortPlan& plan, const uint32_t* ref_counter,
                                     uint32_t capacity, uint2* keys_a, uint32_t* vals_a,
                                     uint2* keys_b, uint32_t* vals_b, uint32_t* status,
                                     uint32_t* g_hist, uint32_t* part_counters, uint32_t* err,
                                     int sm_count, cudaStream_t s);
+// Stable LSD passes of `plan` (word ignored) over 32-bit keys; the histograms
+// are computed here.  count is read on the device.
+cudaError_t launch_sort_u32(const SortPlan& plan, const uint32_t* count, uint32_t capacity,
+                            uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
+                            uint32_t* vals_b, uint32_t* status, uint32_t* g_hist,
+                            uint32_t* part_counters, uint32_t* err, int sm_count, cudaStream_t s);
 // Four 8-bit passes over 32-bit per-splat depth keys (count read on device).
 cudaError_t launch_sort_depth_keys(const uint32_t* count, uint32_t capacity, uint32_t* keys_a,
                                    uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b,
                                    uint32_t* status, uint32_t* g_hist, uint32_t* part_counters,
                                    uint32_t* err, int sm_count, cudaStream_t s);
-// Emit in depth-sorted splat order + histograms of the tile-id digit places.
-cudaError_t launch_emit_sorted(const FrameUniforms* d_frame, uint32_t n,
+// Raster work order: tile indices sorted by decreasing expected cost
+// (schedule = GS3D_SCHEDULE_KEY_COUNT: the tile's key count), so the
+// persistent raster CTAs start the longest tiles first.
+cudaError_t launch_schedule(uint32_t schedule, const uint32_t* tile_offsets, uint32_t num_tiles,
+                            const uint32_t* num_tiles_dev, uint32_t* keys_a, uint32_t* order_a,
+                            uint32_t* keys_b, uint32_t* order_b, uint32_t* status, Ctrl* ctrl,
+                            int sm_count, cudaStream_t s);
+
+// Emit in depth-sorted order over all splat-views of a batch (global tile
+// ids, global splat-view values) + histograms of the tile-id digit places.
+cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t total,
                                const gs3d_projected_splat* proj, const uint32_t* sorted_ids,
                                const uint32_t* sorted_offsets, const uint32_t* ref_counter,
                                uint32_t capacity, uint2* keys, uint32_t* values,
@@ -199,9 +257,23 @@ cudaError_t launch_emit_sorted(const FrameUniforms* d_frame, uint32_t n,
 cudaError_t launch_identify(const uint2* keys, const uint32_t* ref_counter, uint32_t capacity,
                             uint32_t num_tiles, uint32_t* tile_offsets, uint32_t* err,
                             int sm_count, cudaStream_t s);
-cudaError_t launch_raster(const FrameUniforms* d_frame, uint32_t tiles_x, uint32_t tiles_y,
-                          uint32_t tile_w, uint32_t tile_h, const gs3d_projected_splat* proj,
-                          const uint32_t* tile_offsets, const uint32_t* values, uint2* image,
-                          uint32_t* tile_costs, cudaStream_t s);
+// Rasterizes every tile of the batch.  Persistent CTAs pull tile indices
+// from a device work queue (order[k] = k-th tile to render, identity when
+// order is null) through *queue_counter, which must be zero at launch.
+struct RasterArgs {
+  const ViewDesc* views;
+  uint32_t n_views;
+  uint32_t num_tiles;     // total over views
+  uint32_t tile_w, tile_h;
+  const gs3d_projected_splat* proj;
+  const uint32_t* tile_offsets;
+  const uint32_t* values;
+  uint2* image;
+  uint32_t* tile_costs;   // may be null
+  const uint32_t* order;  // may be null
+  uint32_t* queue_counter;
+  bool culled;
+};
+cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s);
 
 }  // namespace gs3d

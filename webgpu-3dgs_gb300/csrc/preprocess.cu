@@ -72,42 +72,42 @@ __device__ __forceinline__ void sh_color(float px, float py, float pz, const flo
   }
 }
 
+// preprocess_splats.wgsl:76-184 for the block's 256 splats of one view.
 template <int DEG>
-__global__ void __launch_bounds__(kThreads)
-    preprocess_kernel(const FrameUniforms* __restrict__ fu, uint32_t n,
-                      const float4* __restrict__ positions, const float4* __restrict__ scales,
-                      const float4* __restrict__ rotations, const float4* __restrict__ colors,
-                      const float* __restrict__ sh_rest, gs3d_projected_splat* __restrict__ out,
-                      uint32_t* __restrict__ counts, uint32_t* __restrict__ depth_keys,
-                      uint32_t* __restrict__ depth_ids, uint32_t* __restrict__ err) {
+__device__ __forceinline__ void preprocess_block(const ViewDesc& vd, uint32_t local_first,
+                                                 float* s_sh, uint64_t* s_bar,
+                                                 gs3d_projected_splat* __restrict__ out,
+                                                 uint32_t* __restrict__ counts,
+                                                 uint32_t* __restrict__ depth_keys,
+                                                 uint32_t* __restrict__ depth_ids,
+                                                 uint32_t* __restrict__ err) {
   constexpr int K = (DEG + 1) * (DEG + 1) - 1;
   constexpr int KC = 3 * K;  // floats of SH rest per splat
-  extern __shared__ __align__(16) float s_sh[];
-  __shared__ uint64_t s_bar;
-
-  const uint32_t first = blockIdx.x * kThreads;
-  const uint32_t i = first + threadIdx.x;
-  const bool active = i < n;
+  const FrameUniforms* fu = &vd.f;
+  const uint32_t n = vd.f.splat_count;
+  const uint32_t li = local_first + threadIdx.x;
+  const bool active = li < n;
+  const uint32_t gi = vd.splat_base + li;  // global splat-view index
 
   // ---- SH slice: one bulk copy per block (issued first, waited on late) ----
   bool bulk = false;
   if (DEG > 0) {
-    const uint32_t cnt = min((uint32_t)kThreads, n - first);
+    const uint32_t cnt = min((uint32_t)kThreads, n - local_first);
     const uint32_t bytes = cnt * KC * 4u;
-    bulk = (bytes % 16u) == 0u;
+    const float* src = vd.sh + (size_t)local_first * KC;
+    bulk = (bytes % 16u) == 0u && (reinterpret_cast<uintptr_t>(src) % 16u) == 0u;
     if (bulk) {
       if (threadIdx.x == 0) {
-        mbar_init(&s_bar, 1);
+        mbar_init(s_bar, 1);
         fence_mbar_init();
       }
       __syncthreads();
       if (threadIdx.x == 0) {
-        mbar_expect_tx(&s_bar, bytes);
-        bulk_g2s(s_sh, sh_rest + (size_t)first * KC, bytes, &s_bar);
+        mbar_expect_tx(s_bar, bytes);
+        bulk_g2s(s_sh, src, bytes, s_bar);
       }
     } else {
-      for (uint32_t k = threadIdx.x; k < cnt * KC; k += kThreads)
-        s_sh[k] = __ldg(sh_rest + (size_t)first * KC + k);
+      for (uint32_t k = threadIdx.x; k < cnt * KC; k += kThreads) s_sh[k] = __ldg(src + k);
       __syncthreads();
     }
   }
@@ -122,10 +122,10 @@ __global__ void __launch_bounds__(kThreads)
   float4 p = r0, col = r0;
 
   if (active) {
-    p = __ldg(positions + i);
-    const float4 s = __ldg(scales + i);
-    const float4 q = __ldg(rotations + i);
-    col = __ldg(colors + i);
+    p = __ldg(vd.pos + li);
+    const float4 s = __ldg(vd.scale + li);
+    const float4 q = __ldg(vd.rot + li);
+    col = __ldg(vd.color + li);
 
     float vp[4], cp[4];
 #pragma unroll
@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(kThreads)
   }
 
   if (DEG > 0) {
-    if (bulk && !mbar_wait(&s_bar, 0)) {
+    if (bulk && !mbar_wait(s_bar, 0)) {
       if (threadIdx.x == 0) latch_error(err, DEVERR_TIMEOUT);
       valid = false;
     }
@@ -251,50 +251,81 @@ __global__ void __launch_bounds__(kThreads)
     } else {
       r2.w = __uint_as_float(1u);
     }
-    float4* o = reinterpret_cast<float4*>(out + i);
+    float4* o = reinterpret_cast<float4*>(out + gi);
     o[0] = r0;
     o[1] = r1;
     o[2] = r2;
     reinterpret_cast<uint4*>(o)[3] = r3;
-    counts[i] = count;
+    counts[gi] = count;
     if (depth_keys != nullptr) {  // per-splat depth sort keys of the fused rebin
-      depth_keys[i] = valid ? __float_as_uint(-r0.z) : 0xffffffffu;
-      depth_ids[i] = i;
+      depth_keys[gi] = valid ? __float_as_uint(-r0.z) : 0xffffffffu;
+      depth_ids[gi] = gi;
     }
+  }
+}
+
+template <int MAXDEG>
+__global__ void __launch_bounds__(kThreads)
+    preprocess_kernel(const ViewDesc* __restrict__ views, uint32_t n_views,
+                      gs3d_projected_splat* __restrict__ out, uint32_t* __restrict__ counts,
+                      uint32_t* __restrict__ depth_keys, uint32_t* __restrict__ depth_ids,
+                      uint32_t* __restrict__ err) {
+  extern __shared__ __align__(16) float s_sh[];
+  __shared__ uint64_t s_bar;
+  const uint32_t v =
+      find_view(n_views, blockIdx.x, [&](uint32_t i) { return __ldg(&views[i].block_base); });
+  const ViewDesc& vd = views[v];
+  const uint32_t local_first = (blockIdx.x - vd.block_base) * kThreads;
+  const uint32_t deg = vd.sh == nullptr ? 0u : min(vd.sh_degree, (uint32_t)MAXDEG);
+  switch (deg) {  // uniform per block
+    case 0:
+      preprocess_block<0>(vd, local_first, s_sh, &s_bar, out, counts, depth_keys, depth_ids, err);
+      break;
+    case 1:
+      if (MAXDEG >= 1)
+        preprocess_block<MAXDEG >= 1 ? 1 : 0>(vd, local_first, s_sh, &s_bar, out, counts,
+                                              depth_keys, depth_ids, err);
+      break;
+    case 2:
+      if (MAXDEG >= 2)
+        preprocess_block<MAXDEG >= 2 ? 2 : 0>(vd, local_first, s_sh, &s_bar, out, counts,
+                                              depth_keys, depth_ids, err);
+      break;
+    default:
+      if (MAXDEG >= 3)
+        preprocess_block<MAXDEG >= 3 ? 3 : 0>(vd, local_first, s_sh, &s_bar, out, counts,
+                                              depth_keys, depth_ids, err);
+      break;
   }
 }
 
 }  // namespace
 
-cudaError_t launch_preprocess(const FrameUniforms* d_frame, uint32_t n, const float4* pos,
-                              const float4* scale, const float4* rot, const float4* color,
-                              const float* sh_rest, uint32_t sh_degree,
-                              gs3d_projected_splat* out, uint32_t* counts, uint32_t* depth_keys,
-                              uint32_t* depth_ids, uint32_t* err, cudaStream_t s) {
-  const uint32_t blocks = (n + kThreads - 1) / kThreads;
-  if (blocks == 0) return cudaSuccess;
-  if (sh_rest == nullptr) sh_degree = 0;
-  const uint32_t kc = 3u * ((sh_degree + 1) * (sh_degree + 1) - 1);
+cudaError_t launch_preprocess(const ViewDesc* views, uint32_t n_views, uint32_t total_blocks,
+                              uint32_t max_sh_degree, gs3d_projected_splat* out, uint32_t* counts,
+                              uint32_t* depth_keys, uint32_t* depth_ids, uint32_t* err,
+                              cudaStream_t s) {
+  if (total_blocks == 0) return cudaSuccess;
+  const uint32_t kc = 3u * ((max_sh_degree + 1) * (max_sh_degree + 1) - 1);
+  // 45 floats x 256 splats = 46,080 B at degree 3: inside the 48 KB default window
   const size_t smem = (size_t)kc * kThreads * sizeof(float);
-  switch (sh_degree) {
+  switch (max_sh_degree) {
     case 0:
-      preprocess_kernel<0><<<blocks, kThreads, 0, s>>>(d_frame, n, pos, scale, rot, color, nullptr,
-                                                       out, counts, depth_keys, depth_ids, err);
+      preprocess_kernel<0><<<total_blocks, kThreads, 0, s>>>(views, n_views, out, counts,
+                                                             depth_keys, depth_ids, err);
       break;
     case 1:
-      preprocess_kernel<1><<<blocks, kThreads, smem, s>>>(d_frame, n, pos, scale, rot, color,
-                                                          sh_rest, out, counts, depth_keys, depth_ids, err);
+      preprocess_kernel<1><<<total_blocks, kThreads, smem, s>>>(views, n_views, out, counts,
+                                                                depth_keys, depth_ids, err);
       break;
     case 2:
-      preprocess_kernel<2><<<blocks, kThreads, smem, s>>>(d_frame, n, pos, scale, rot, color,
-                                                          sh_rest, out, counts, depth_keys, depth_ids, err);
+      preprocess_kernel<2><<<total_blocks, kThreads, smem, s>>>(views, n_views, out, counts,
+                                                                depth_keys, depth_ids, err);
       break;
-    default: {
-      // 45 floats x 256 splats = 46,080 B: inside the 48 KB default window.
-      preprocess_kernel<3><<<blocks, kThreads, smem, s>>>(d_frame, n, pos, scale, rot, color,
-                                                          sh_rest, out, counts, depth_keys, depth_ids, err);
+    default:
+      preprocess_kernel<3><<<total_blocks, kThreads, smem, s>>>(views, n_views, out, counts,
+                                                                depth_keys, depth_ids, err);
       break;
-    }
   }
   return cudaGetLastError();
 }

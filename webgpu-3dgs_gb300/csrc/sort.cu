@@ -59,8 +59,8 @@ struct KeyOps<uint32_t> {
 };
 
 template <typename K>
-constexpr size_t pass_smem() {
-  return (size_t)kPart * (sizeof(K) + sizeof(uint32_t)) +
+constexpr size_t pass_smem() {  // two partition buffers + per-warp histograms
+  return 2 * (size_t)kPart * (sizeof(K) + sizeof(uint32_t)) +
          (size_t)kWarps * kRadixBins * sizeof(uint32_t);
 }
 
@@ -149,48 +149,94 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 template <typename K>
+constexpr size_t part_buf_bytes() {
+  return (size_t)kPart * (sizeof(K) + sizeof(uint32_t));
+}
+
+// One LSD pass.  Persistent CTAs claim 4096-key partitions in order and
+// double-buffer them: the partition after the current one is fetched by two
+// bulk (TMA) copies into the other shared-memory buffer while the current one
+// is ranked, reordered and written out.  Claiming one partition ahead cannot
+// deadlock: the smallest unfinished partition is always some CTA's current
+// one, and it waits only on smaller, finished partitions.
+template <typename K>
 __global__ void __launch_bounds__(kThreads, 2)
     onesweep_kernel(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                     const uint32_t* __restrict__ ref_counter, uint32_t capacity, int word,
                     int shift, const uint32_t* __restrict__ hist, uint32_t* __restrict__ status,
                     uint32_t* __restrict__ part_counter, uint32_t* __restrict__ err) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  K* s_keys = reinterpret_cast<K*>(smem);
-  uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + kPart);
-  uint32_t* s_whist = s_vals + kPart;  // [kWarps][256]
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr size_t kBuf = part_buf_bytes<K>();
+  uint32_t* s_whist = reinterpret_cast<uint32_t*>(smem + 2 * kBuf);  // [kWarps][256]
   __shared__ uint32_t s_bucket[kRadixBins], s_dstart[kRadixBins], s_dest[kRadixBins];
   __shared__ uint32_t s_wsum[kWarps];
-  __shared__ uint32_t s_part;
+  __shared__ uint32_t s_next;
+  __shared__ uint64_t s_bar[2];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t R = live_refs(ref_counter, capacity);
   const uint32_t num_parts = (R + kPart - 1) / kPart;
 
+  auto issue = [&](uint32_t part, int b) {  // thread 0 only
+    unsigned char* buf = smem + b * kBuf;
+    const uint32_t kb = kPart * sizeof(K), vb = kPart * sizeof(uint32_t);
+    mbar_expect_tx(&s_bar[b], kb + vb);
+    bulk_g2s(buf, keys_in + (size_t)part * kPart, kb, &s_bar[b]);
+    bulk_g2s(buf + kb, vals_in + (size_t)part * kPart, vb, &s_bar[b]);
+  };
+
   // global bucket bases of this digit place
   s_bucket[tid] = block_exclusive_256(__ldg(hist + tid), s_wsum);
+  if (tid == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    fence_mbar_init();
+    s_next = atomicAdd(part_counter, 1u);
+    if (s_next < num_parts) issue(s_next, 0);
+  }
+  __syncthreads();
+  uint32_t cur = s_next;
+  int b = 0;
+  uint32_t phase0 = 0, phase1 = 0;
 
-  while (true) {
-    __syncthreads();  // previous partition fully written out
-    if (tid == 0) s_part = atomicAdd(part_counter, 1u);
-    for (int k = tid; k < kWarps * kRadixBins; k += kThreads) s_whist[k] = 0u;
+  while (cur < num_parts) {
+    // claim the next partition and fetch it into the other buffer, whose
+    // previous contents were fully written out before this barrier
     __syncthreads();
-    const uint32_t part = s_part;
-    if (part >= num_parts) break;
+    if (tid == 0) {
+      const uint32_t nxt = atomicAdd(part_counter, 1u);
+      s_next = nxt;
+      if (nxt < num_parts) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(nxt, b ^ 1);
+      }
+    }
+    for (int k = tid; k < kWarps * kRadixBins; k += kThreads) s_whist[k] = 0u;
+    K* s_keys = reinterpret_cast<K*>(smem + b * kBuf);
+    uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + b * kBuf + kPart * sizeof(K));
+    const bool landed = mbar_wait(&s_bar[b], b ? phase1 : phase0);
+    if (b) phase1 ^= 1u; else phase0 ^= 1u;
+    if (!__syncthreads_and(landed)) {  // bounded wait gave up: stop this CTA
+      if (tid == 0) latch_error(err, DEVERR_TIMEOUT);
+      break;
+    }
+    const uint32_t nxt = s_next;
+    const uint32_t part = cur;
     const uint32_t base = part * kPart;
     const uint32_t count = min(kPart, R - base);
 
-    // ---- load (warp-striped: lane-contiguous, coalesced) ----
+    // ---- registers <- shared (warp-striped: lane-contiguous) ----
     K key[kItems];
     uint32_t val[kItems];
     uint32_t dr[kItems];  // digit | rank-in-warp << 8
-    const uint32_t wbase = base + warp * (32u * kItems);
+    const uint32_t wloc = warp * (32u * kItems);
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
-      const uint32_t idx = wbase + i * 32u + lane;
-      if (idx < R) {
-        key[i] = keys_in[idx];
-        val[i] = __ldg(vals_in + idx);
+      const uint32_t loc = wloc + i * 32u + lane;
+      if (loc < count) {
+        key[i] = s_keys[loc];
+        val[i] = s_vals[loc];
       } else {
         key[i] = KeyOps<K>::sentinel();  // digit 255, ranked last
         val[i] = 0u;
@@ -209,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, 2)
       __syncwarp();
       dr[i] = d | ((prior + __popc(peers & lt)) << 8);
     }
-    __syncthreads();
+    __syncthreads();  // histograms complete; every item read out of the buffer
 
     // ---- per digit (thread = digit): warp offsets, partition totals ----
     uint32_t run = 0;
@@ -226,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     s_dstart[tid] = dstart;
     __syncthreads();
 
-    // ---- reorder the partition in shared memory ----
+    // ---- reorder the partition in place ----
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const uint32_t d = dr[i] & 0xffu;
@@ -259,22 +305,23 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
     s_dest[tid] = s_bucket[tid] + excl - dstart;
     const int all_ok = __syncthreads_and(ok);
-    if (!all_ok) {
-      if (tid == 0) latch_error(err, DEVERR_TIMEOUT);
-      continue;  // nothing written for this partition
-    }
-
-    // ---- write each digit run contiguously ----
-    for (uint32_t j = tid; j < count; j += kThreads) {
-      const K k = s_keys[j];
-      const uint32_t dst = s_dest[KeyOps<K>::digit(k, word, shift)] + j;
-      if (dst < R) {
-        keys_out[dst] = k;
-        vals_out[dst] = s_vals[j];
-      } else {
-        latch_error(err, DEVERR_RANGE);
+    if (all_ok) {
+      // ---- write each digit run contiguously ----
+      for (uint32_t j = tid; j < count; j += kThreads) {
+        const K k = s_keys[j];
+        const uint32_t dst = s_dest[KeyOps<K>::digit(k, word, shift)] + j;
+        if (dst < R) {
+          keys_out[dst] = k;
+          vals_out[dst] = s_vals[j];
+        } else {
+          latch_error(err, DEVERR_RANGE);
+        }
       }
+    } else if (tid == 0) {
+      latch_error(err, DEVERR_TIMEOUT);  // nothing written for this partition
     }
+    cur = nxt;
+    b ^= 1;
   }
 }
 
@@ -386,6 +433,10 @@ SortPlan make_sort_plan(uint32_t num_tiles) {
   return p;
 }
 
+uint32_t sort_capacity_round(uint32_t capacity) {
+  return (uint32_t)(((uint64_t)capacity + kPart - 1) / kPart * kPart);
+}
+
 size_t sort_status_words(uint32_t capacity, int passes) {
   const size_t parts = ((size_t)capacity + kPart - 1) / kPart + 1;
   return parts * kRadixBins * (size_t)passes;
@@ -411,6 +462,14 @@ cudaError_t launch_sort_tile_passes(const SortPlan& plan, const uint32_t* ref_co
                                     int sm_count, cudaStream_t s) {
   return run_passes<uint2>(plan, ref_counter, capacity, keys_a, vals_a, keys_b, vals_b, status,
                            g_hist, part_counters, err, true, sm_count, s);
+}
+
+cudaError_t launch_sort_u32(const SortPlan& plan, const uint32_t* count, uint32_t capacity,
+                            uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b,
+                            uint32_t* vals_b, uint32_t* status, uint32_t* g_hist,
+                            uint32_t* part_counters, uint32_t* err, int sm_count, cudaStream_t s) {
+  return run_passes<uint32_t>(plan, count, capacity, keys_a, vals_a, keys_b, vals_b, status,
+                              g_hist, part_counters, err, false, sm_count, s);
 }
 
 cudaError_t launch_sort_depth_keys(const uint32_t* count, uint32_t capacity, uint32_t* keys_a,

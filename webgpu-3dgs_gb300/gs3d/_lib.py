@@ -60,6 +60,20 @@ class Config_t(C.Structure):
                 ("flags", C.c_uint32)]
 
 
+class View_t(C.Structure):
+    _fields_ = [("camera", Camera_t), ("scene", C.c_uint32), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class ViewInfo_t(C.Structure):
+    _fields_ = [("pixel_offset", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("tiles_x", C.c_uint32), ("tiles_y", C.c_uint32), ("tile_base", C.c_uint32),
+                ("splat_base", C.c_uint32), ("splat_count", C.c_uint32), ("scene", C.c_uint32)]
+
+
+SCHEDULE_ROW_MAJOR = 0
+SCHEDULE_KEY_COUNT = 1
+
 assert C.sizeof(Camera_t) == 288
 
 # every entry point declared in include/gs3d.h, with its ctypes signature
@@ -70,6 +84,10 @@ SIGNATURES = {
     "gs3d_destroy": ([_P], _I),
     "gs3d_last_error": ([_P], C.c_char_p),
     "gs3d_set_splats": ([_P, _U32, _P, _P, _P, _P, _P, _U32, _I], _I),
+    "gs3d_add_scene": ([_P, _U32, _P, _P, _P, _P, _P, _U32, _I, C.POINTER(_U32)], _I),
+    "gs3d_rebin_batch": ([_P, _P, _U32], _I),
+    "gs3d_get_view_info": ([_P, _U32, C.POINTER(ViewInfo_t)], _I),
+    "gs3d_set_schedule": ([_P, _U32], _I),
     "gs3d_set_tile_size": ([_P, _U32, _U32, C.POINTER(_U32), C.POINTER(_U32)], _I),
     "gs3d_set_camera": ([_P, C.POINTER(Camera_t), _U32, _U32], _I),
     "gs3d_preprocess": ([_P], _I),

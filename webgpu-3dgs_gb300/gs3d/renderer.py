@@ -138,6 +138,10 @@ class GaussianSplatRenderer:
         values, tile ranges and images."""
         self._call("gs3d_set_flags", _lib.FLAG_STAGEWISE_REBIN if on else 0)
 
+    def setSchedule(self, schedule: int) -> None:
+        """Raster work order: _lib.SCHEDULE_ROW_MAJOR or SCHEDULE_KEY_COUNT."""
+        self._call("gs3d_set_schedule", int(schedule))
+
     def setAlwaysRebin(self, on: bool) -> None:
         self.alwaysRebin = bool(on)
 
@@ -194,6 +198,78 @@ class GaussianSplatRenderer:
             _check(self.lib, self.ctx, rc)
             return
         _check(self.lib, self.ctx, rc)
+
+    # ---- batched rendering (extension) -----------------------------------------
+    def addScene(self, data: GaussianSplatData) -> int:
+        """Makes another scene resident; returns its id for batched views."""
+        arrs = [np.ascontiguousarray(a, np.float32) for a in
+                (data.positions, data.scales, data.rotations, data.colors)]
+        deg = int(data.sphericalHarmonicsDegree)
+        sh = np.ascontiguousarray(data.sphericalHarmonics, np.float32) if deg > 0 else None
+        ptr = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        out = C.c_uint32()
+        self._call("gs3d_add_scene", data.splatCount, *(ptr(a) for a in arrs), ptr(sh), deg, 0,
+                   C.byref(out))
+        if self.scene.splats is None:
+            self.scene.splats = data
+        return int(out.value)
+
+    def rebinBatch(self, views, check: bool = True) -> None:
+        """views: iterable of (scene_id, camera_uniform_72, width, height)."""
+        views = list(views)
+        arr = (_lib.View_t * len(views))()
+        for i, (scene, u, w, h) in enumerate(views):
+            arr[i].camera = camera_struct(u)
+            arr[i].scene = int(scene)
+            arr[i].width = int(w)
+            arr[i].height = int(h)
+        self._batch = len(views)
+        for _ in range(3):
+            self._call("gs3d_rebin_batch", C.cast(arr, C.c_void_p), len(views))
+            if not check:
+                return
+            rc = self.lib.gs3d_synchronize(self.ctx)
+            if rc == _lib.ERR_CAPACITY:
+                continue
+            _check(self.lib, self.ctx, rc)
+            return
+        _check(self.lib, self.ctx, rc)
+
+    def viewInfo(self, v: int) -> _lib.ViewInfo_t:
+        info = _lib.ViewInfo_t()
+        self._call("gs3d_get_view_info", int(v), C.byref(info))
+        return info
+
+    def readViewImage(self, v: int) -> np.ndarray:
+        info = self.viewInfo(v)
+        n = (info.pixel_offset + info.width * info.height) * 4
+        flat = np.zeros(n, np.float16)
+        self._call("gs3d_read_buffer", _lib.BUFFERS["splat_target"],
+                   flat.ctypes.data_as(C.c_void_p), flat.nbytes)
+        return flat[info.pixel_offset * 4:].reshape(info.height, info.width, 4)
+
+    def readViewRefs(self, v: int):
+        """(keys, values, tile counts) of view v in single-view terms: tile ids
+        relative to the view, values as scene splat ids."""
+        info = self.viewInfo(v)
+        R = self.refCount()
+        keys = self.readBuffer("sort_keys_a", R)
+        vals = self.readBuffer("sort_values_a", R)
+        t0, t1 = info.tile_base, info.tile_base + info.tiles_x * info.tiles_y
+        a, b = np.searchsorted(keys[:, 0], [t0, t1])
+        k = keys[a:b].copy()
+        k[:, 0] -= t0
+        total = self._total_tiles()
+        off = np.zeros(total + 1, np.uint32)
+        self._call("gs3d_read_buffer", _lib.BUFFERS["tile_offsets"],
+                   off.ctypes.data_as(C.c_void_p), off.nbytes)
+        o = off.astype(np.int64)
+        counts = np.maximum(o[t0 + 1:t1 + 1] - o[t0:t1], 0)
+        return k, vals[a:b] - info.splat_base, counts
+
+    def _total_tiles(self) -> int:
+        last = self.viewInfo(self._batch - 1)
+        return last.tile_base + last.tiles_x * last.tiles_y
 
     # ---- individual stages (for stage-wise parity) --------------------------
     def setCamera(self, camera_uniform, width, height) -> None:
