@@ -435,6 +435,7 @@ SortPlan tile_digit_plan(uint32_t num_tiles) {
   for (int p = 4; p < full.passes; ++p) {  // the tile-id digit places only
     tp.word[tp.passes] = full.word[p];
     tp.shift[tp.passes] = full.shift[p];
+    tp.nbits[tp.passes] = full.nbits[p];
     ++tp.passes;
   }
   return tp;

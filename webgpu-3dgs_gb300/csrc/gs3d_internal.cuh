@@ -190,9 +190,10 @@ __device__ __forceinline__ uint32_t live_refs(const uint32_t* ref_counter, uint3
 // ---------------------------------------------------------------------------
 // Host-side launchers (one translation unit per stage).
 struct SortPlan {
-  int passes;                    // number of 8-bit digit passes
+  int passes;                    // number of digit passes (digits of up to 8 bits)
   int word[kMaxSortPasses];      // 0 = hi (tile id), 1 = lo (depth bits)
   int shift[kMaxSortPasses];
+  int nbits[kMaxSortPasses];     // significant bits of the digit (0 = 8)
 };
 SortPlan make_sort_plan(uint32_t num_tiles);
 

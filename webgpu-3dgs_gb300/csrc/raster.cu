@@ -14,20 +14,25 @@
 //    current one is blended;
 //  * the CTA leaves as soon as a block-wide vote finds every pixel
 //    terminated (the reference keeps looping over the remaining batches);
+//  * each staged splat is converted once per tile into pre-scaled conic
+//    coefficients, so a (pixel, splat) pair costs one ex2 and a branch-free
+//    handful of FMAs (a skipped splat blends with alpha = 0, which leaves the
+//    pixel bit-unchanged);
 //  * (culled variant) each warp owns a compact pixel block (8x4 for tiles
 //    whose sides divide by 8 and 4) and tests every staged splat once against
-//    it; a splat is skipped for the whole warp only when every pixel of the
-//    block is provably rejected by the per-pixel tests themselves: outside
-//    the radius circle, or alpha < 1/255 by the bound
-//    alpha <= opacity * exp(-0.5 * lambda_min(conic) * |d|^2), both with
-//    margins that cover f32 rounding.  Pixels therefore blend exactly the
-//    same splats in the same order, and the image is bit-identical to the
-//    one-thread-per-pixel variant;
+//    it; a splat is skipped for the whole warp only when no pixel centre of
+//    the block can pass the per-pixel tests: the block lies outside the
+//    radius circle, or the exact minimum of d^T conic d over the block keeps
+//    alpha below 1/255, with margins that cover f32 rounding.  Pixels
+//    therefore blend exactly the same splats in the same order, and the
+//    image is bit-identical to the one-thread-per-pixel variant;
 //  * each CTA records the tile's cost: the number of splats iterated before
 //    its last pixel terminated.
 //
-// The per-pixel update is written with explicit round-to-nearest intrinsics so
-// both variants compile to the same arithmetic.
+// Both variants call the same per-pixel function, so they compile to the same
+// arithmetic.  Against the reference's f32 expression order the per-pixel
+// math differs only in rounding (log2-domain exponent, fused multiply-adds),
+// which the 2/255 image tolerance covers.
 #include <algorithm>
 
 #include "gs3d_internal.cuh"
@@ -35,38 +40,64 @@
 namespace gs3d {
 namespace {
 
-struct SplatStage {  // first 48 bytes of a ProjectedSplat
-  float4 a;  // mean_px.xy, depth, radius_px
-  float4 b;  // conic.xyz, opacity
-  float4 c;  // color.xyz, valid
+struct SplatStage {  // first 48 bytes of a ProjectedSplat, prepared in place (prepare())
+  float4 a;  // mean_px.x, mean_px.y, radius_px^2, opacity
+  float4 b;  // qa, qb, qc, vis: Q(d) = qa dx^2 + qb dx dy + qc dy^2 = log2(e)/2 * d^T conic d
+  float4 c;  // color.xyz, unused
 };
 
 struct Pixel {
   float cr, cg, cb, T;
 };
 
-// rasterize_tiles.wgsl:81-98 for one (pixel, splat) pair; true once the
-// pixel's transmittance fell below 1e-4.
-__device__ __forceinline__ bool blend_one(float pfx, float pfy, const SplatStage& s, Pixel& p) {
-  const float4 a = s.a;
-  const float dx = __fsub_rn(pfx, a.x);
-  const float dy = __fsub_rn(pfy, a.y);
-  if (__fmaf_rn(dx, dx, __fmul_rn(dy, dy)) > __fmul_rn(a.w, a.w)) return false;
-  const float4 b = s.b;
-  const float q = __fmaf_rn(__fmul_rn(b.x, dx), dx,
-                            __fmaf_rn(__fmul_rn(__fmul_rn(2.0f, b.y), dx), dy,
-                                      __fmul_rn(__fmul_rn(b.z, dy), dy)));
-  const float power = __fmul_rn(-0.5f, q);
-  if (power > 0.0f) return false;
-  const float alpha = fminf(0.99f, __fmul_rn(b.w, __expf(power)));
-  if (alpha < 1.0f / 255.0f) return false;
+// ex2.approx: 2^x on the SFU.
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Converts the staged ProjectedSplat prefix (mean, depth, radius | conic,
+// opacity | color, valid) into the raster form.  vis = the largest Q at which
+// alpha can still reach 1/255, with a 1% margin (-1: never visible; +inf:
+// conic too ill-conditioned for the alpha bound, use the circle only).
+__device__ __forceinline__ void prepare(SplatStage& s) {
+  const float4 a = s.a, b = s.b;
+  const float k = 0.72134752044448170f;  // log2(e) / 2
+  const float A = b.x, B = b.y, C = b.z, op = b.w;
+  float vis;
+  const float lim = op * 255.0f;
+  if (!(lim > 1.0f)) {
+    vis = -1.0f;  // alpha = opacity * exp(power) <= opacity < 1/255 everywhere
+  } else if (A * C - B * B >= 1e-3f * (A + C) * (A + C) && A > 0.0f && C > 0.0f) {
+    vis = __log2f(lim) * 1.01f + 1e-3f;
+  } else {
+    vis = __int_as_float(0x7f800000);
+  }
+  s.a = make_float4(a.x, a.y, a.w * a.w, op);
+  s.b = make_float4(k * A, 2.0f * k * B, k * C, vis);
+}
+
+// rasterize_tiles.wgsl:81-98 for one (pixel, splat) pair, branch-free: a
+// skipped splat contributes alpha = 0, which leaves C and T bit-unchanged.
+// Returns true when the pixel terminates at this splat.
+__device__ __forceinline__ bool blend_one(float pfx, float pfy, const SplatStage& s, Pixel& p,
+                                          bool live) {
+  const float4 a = s.a, b = s.b;
+  const float dx = pfx - a.x;
+  const float dy = pfy - a.y;
+  const float d2 = fmaf(dx, dx, dy * dy);
+  const float Q = fmaf(b.x * dx, dx, fmaf(b.y * dx, dy, b.z * dy * dy));  // = -power * log2(e)
+  const float alpha = fminf(0.99f, a.w * ex2_approx(-Q));
+  const bool ok = live && (d2 <= a.z) && (Q >= 0.0f) && (alpha >= 1.0f / 255.0f);
+  const float al = ok ? alpha : 0.0f;
   const float4 c = s.c;
-  const float ta = __fmul_rn(p.T, alpha);
-  p.cr = __fmaf_rn(ta, c.x, p.cr);
-  p.cg = __fmaf_rn(ta, c.y, p.cg);
-  p.cb = __fmaf_rn(ta, c.z, p.cb);
-  p.T = __fmul_rn(p.T, __fsub_rn(1.0f, alpha));
-  return p.T < 1.0e-4f;
+  const float ta = p.T * al;
+  p.cr = fmaf(ta, c.x, p.cr);
+  p.cg = fmaf(ta, c.y, p.cg);
+  p.cb = fmaf(ta, c.z, p.cb);
+  p.T = p.T * (1.0f - al);
+  return ok && p.T < 1.0e-4f;
 }
 
 __device__ __forceinline__ void store_pixel(uint2* image, uint32_t W, uint32_t px, uint32_t py,
@@ -88,6 +119,31 @@ __device__ __forceinline__ void stage_batch(const gs3d_projected_splat* __restri
     cp_async16(&dst->c, src + 2);
   }
   cp_async_commit();
+}
+
+// Can the splat reach alpha >= 1/255 inside the rectangle of pixel centres
+// [x0,x1] x [y0,y1]?  Exact minimum of Q over the rectangle (the quadratic
+// form's minimum over a box not holding the mean lies on an edge, at the
+// clamped stationary point of that edge), compared with vis; plus the radius
+// circle.  Conservative by the margins folded into vis and the circle.
+__device__ __forceinline__ bool rect_may_hit(const SplatStage& s, float xlo, float xhi, float ylo,
+                                             float yhi) {
+  const float4 a = s.a, b = s.b;
+  const float x0 = xlo - a.x, x1 = xhi - a.x, y0 = ylo - a.y, y1 = yhi - a.y;
+  const float ex = fminf(fmaxf(0.0f, x0), x1), ey = fminf(fmaxf(0.0f, y0), y1);
+  if (ex * ex + ey * ey > a.z * 1.0001f + 1e-3f) return false;
+  const float vis = b.w;
+  if (vis < 0.0f) return false;
+  if (ex == 0.0f && ey == 0.0f) return true;  // the mean lies inside
+  if (vis == __int_as_float(0x7f800000)) return true;
+  const float qa = b.x, qb = b.y, qc = b.z;
+  auto Q = [&](float x, float y) { return fmaf(qa * x, x, fmaf(qb * x, y, qc * y * y)); };
+  const float sy = -qb / (2.0f * qc), sx = -qb / (2.0f * qa);  // edge stationary points
+  float m = Q(x0, fminf(fmaxf(sy * x0, y0), y1));
+  m = fminf(m, Q(x1, fminf(fmaxf(sy * x1, y0), y1)));
+  m = fminf(m, Q(fminf(fmaxf(sx * y0, x0), x1), y0));
+  m = fminf(m, Q(fminf(fmaxf(sx * y1, x0), x1), y1));
+  return m <= vis;
 }
 
 struct TileGeom {
@@ -142,11 +198,12 @@ __device__ void raster_tile_plain(const RasterArgs& a, const TileGeom& g, SplatS
     } else {
       cp_async_wait<0>();
     }
-    __syncthreads();
     const uint32_t cnt = min(nt, end - (start + bi * nt));
+    if (tid < cnt) prepare(cur[tid]);  // own copy is complete
+    __syncthreads();
     if (!done) {
       for (uint32_t j = 0; j < cnt; ++j) {
-        if (blend_one(pfx, pfy, cur[j], p)) {
+        if (blend_one(pfx, pfy, cur[j], p, true)) {
           done = true;
           used = bi * nt + j + 1;
           break;
@@ -165,30 +222,11 @@ __device__ void raster_tile_plain(const RasterArgs& a, const TileGeom& g, SplatS
   }
 }
 
-// Squared distance below which a splat may still touch some pixel of a
-// warp's block (conservative; see the file comment).
-__device__ __forceinline__ float reach_d2(const SplatStage& s) {
-  const float r = s.a.w;
-  const float circle = r * r * 1.0001f + 1e-3f;
-  const float A = s.b.x, B = s.b.y, Cc = s.b.z, op = s.b.w;
-  // smallest eigenvalue of the conic, shrunk to cover its rounding
-  const float h = 0.5f * (A - Cc);
-  float lmin = 0.5f * (A + Cc) - sqrtf(h * h + B * B);
-  lmin = lmin * 0.999f - 1e-7f * (fabsf(A) + fabsf(Cc));
-  const float lim = op * (255.0f * 1.001f);  // alpha >= 1/255 needs exp(power) >= 1/lim
-  if (!(lim > 1.0f)) return -1.0f;           // alpha < 1/255 at every pixel
-  // very elongated conics: the rounding of d^T conic d could exceed the
-  // bound's margin, so only the circle test is used
-  if (!(lmin > 1e-4f * (fabsf(A) + fabsf(Cc)))) return circle;
-  const float alpha_d2 = 2.0f * logf(lim) / lmin * 1.001f + 1e-3f;
-  return fminf(circle, alpha_d2);
-}
-
 // Culled variant: warps own compact pixel blocks and skip splats that no
 // pixel of their block can blend.  blockDim.x == tile_w * tile_h, a multiple
 // of 32.
 __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, SplatStage* buf0,
-                                   SplatStage* buf1, float* s_reach, uint32_t* s_cost) {
+                                   SplatStage* buf1, uint32_t* s_cost) {
   const uint32_t nt = a.tile_w * a.tile_h;
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   uint32_t lx, ly;
@@ -234,23 +272,17 @@ __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, Splat
       cp_async_wait<0>();
     }
     const uint32_t cnt = min(nt, end - (start + bi * nt));
-    if (tid < cnt) s_reach[tid] = reach_d2(cur[tid]);  // own copy is complete
+    if (tid < cnt) prepare(cur[tid]);  // own copy is complete
     __syncthreads();
     if (__any_sync(0xffffffffu, !done)) {
       for (uint32_t k0 = 0; k0 < cnt; k0 += 32) {
         const uint32_t j = k0 + lane;
-        bool hit = false;
-        if (j < cnt) {
-          const float mx = cur[j].a.x, my = cur[j].a.y;
-          const float ex = mx - fminf(fmaxf(mx, xlo), xhi);
-          const float ey = my - fminf(fmaxf(my, ylo), yhi);
-          hit = ex * ex + ey * ey <= s_reach[j];
-        }
+        const bool hit = j < cnt && rect_may_hit(cur[j], xlo, xhi, ylo, yhi);
         uint32_t mask = __ballot_sync(0xffffffffu, hit);
         while (mask) {
           const uint32_t b = __ffs(mask) - 1;
           mask &= mask - 1;
-          if (!done && blend_one(pfx, pfy, cur[k0 + b], p)) {
+          if (blend_one(pfx, pfy, cur[k0 + b], p, !done)) {
             done = true;
             used = bi * nt + k0 + b + 1;
           }
@@ -277,7 +309,6 @@ __global__ void raster_kernel(RasterArgs a) {
   const uint32_t nt = a.tile_w * a.tile_h;
   SplatStage* buf0 = reinterpret_cast<SplatStage*>(smem);
   SplatStage* buf1 = buf0 + nt;
-  float* s_reach = reinterpret_cast<float*>(buf1 + nt);
   __shared__ uint32_t s_item, s_cost;
   while (true) {
     if (threadIdx.x == 0) {
@@ -290,7 +321,7 @@ __global__ void raster_kernel(RasterArgs a) {
     const uint32_t t = a.order != nullptr ? __ldg(a.order + item) : item;
     const TileGeom g = tile_geom(a, t);
     if (CULLED)
-      raster_tile_culled(a, g, buf0, buf1, s_reach, &s_cost);
+      raster_tile_culled(a, g, buf0, buf1, &s_cost);
     else
       raster_tile_plain(a, g, buf0, buf1, &s_cost);
     __syncthreads();  // s_cost complete; shared buffers free for the next tile
@@ -304,7 +335,7 @@ cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s) {
   if (a.num_tiles == 0) return cudaSuccess;
   const uint32_t nt = a.tile_w * a.tile_h;
   const bool culled = a.culled && (nt % 32 == 0);
-  const size_t smem = 2 * (size_t)nt * sizeof(SplatStage) + (culled ? nt * sizeof(float) : 0);
+  const size_t smem = 2 * (size_t)nt * sizeof(SplatStage);
   auto kern = culled ? raster_kernel<true> : raster_kernel<false>;
   // launch configuration per (variant, tile area), computed once per process
   static int cache[2][1025] = {};

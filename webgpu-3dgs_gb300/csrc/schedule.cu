@@ -50,6 +50,7 @@ cudaError_t launch_schedule(uint32_t schedule, const uint32_t* tile_offsets, uin
   plan.word[0] = plan.word[1] = 1;
   plan.shift[0] = 0;
   plan.shift[1] = 8;
+  plan.nbits[0] = plan.nbits[1] = 8;
   // two passes: the result is back in keys_a / order_a
   return launch_sort_u32(plan, num_tiles_dev, num_tiles, keys_a, order_a, keys_b, order_b,
                          status, &ctrl->sched_hist[0][0], ctrl->sched_counter, &ctrl->error,

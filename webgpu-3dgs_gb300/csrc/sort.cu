@@ -34,10 +34,11 @@
 namespace gs3d {
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kWarps = kThreads / 32;
-constexpr int kItems = 16;
-constexpr uint32_t kPart = kThreads * kItems;  // 4096 keys per partition
+constexpr int kThreads = 256;   // histogram kernel
+constexpr int kPassThreads = 512;                  // onesweep pass
+constexpr int kWarps = kPassThreads / 32;          // 16
+constexpr int kItems = 8;
+constexpr uint32_t kPart = kPassThreads * kItems;  // 4096 keys per partition
 constexpr uint32_t kFlagAgg = 1u, kFlagInc = 2u;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
 
@@ -59,9 +60,9 @@ struct KeyOps<uint32_t> {
 };
 
 template <typename K>
-constexpr size_t pass_smem() {  // two partition buffers + per-warp histograms
+constexpr size_t pass_smem() {  // two partition buffers + per-warp u16 histograms
   return 2 * (size_t)kPart * (sizeof(K) + sizeof(uint32_t)) +
-         (size_t)kWarps * kRadixBins * sizeof(uint32_t);
+         (size_t)kWarps * kRadixBins * sizeof(uint16_t);
 }
 
 __device__ __forceinline__ uint32_t warp_inclusive(uint32_t x, int lane) {
@@ -73,27 +74,29 @@ __device__ __forceinline__ uint32_t warp_inclusive(uint32_t x, int lane) {
   return x;
 }
 
-// Exclusive scan of one value per thread over a 256-thread block.
+// Exclusive scan over the first 256 threads' values (one per digit); every
+// thread of the block must call it, threads >= 256 pass 0 and get garbage.
 __device__ __forceinline__ uint32_t block_exclusive_256(uint32_t x, uint32_t* s_wsum) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t inc = warp_inclusive(x, lane);
   __syncthreads();  // s_wsum may still be read from a previous call
-  if (lane == 31) s_wsum[warp] = inc;
+  if (lane == 31 && warp < 8) s_wsum[warp] = inc;
   __syncthreads();
   if (warp == 0) {
-    const uint32_t w = lane < kWarps ? s_wsum[lane] : 0u;
+    const uint32_t w = lane < 8 ? s_wsum[lane] : 0u;
     const uint32_t wi = warp_inclusive(w, lane);
-    if (lane < kWarps) s_wsum[lane] = wi - w;
+    if (lane < 8) s_wsum[lane] = wi - w;
   }
   __syncthreads();
-  return s_wsum[warp] + inc - x;
+  return warp < 8 ? s_wsum[warp] + inc - x : 0u;
 }
 
-// Mask of lanes whose 8-bit digit equals this lane's.
-__device__ __forceinline__ uint32_t match_digit8(uint32_t d) {
+// Mask of lanes whose digit equals this lane's (digits below 2^NBITS).
+template <int NBITS>
+__device__ __forceinline__ uint32_t match_digit(uint32_t d) {
   uint32_t peers = 0xffffffffu;
 #pragma unroll
-  for (int b = 0; b < 8; ++b) {
+  for (int b = 0; b < NBITS; ++b) {
     const uint32_t bit = (d >> b) & 1u;
     const uint32_t bal = __ballot_sync(0xffffffffu, bit);
     peers &= bit ? bal : ~bal;
@@ -159,8 +162,8 @@ constexpr size_t part_buf_bytes() {
 // is ranked, reordered and written out.  Claiming one partition ahead cannot
 // deadlock: the smallest unfinished partition is always some CTA's current
 // one, and it waits only on smaller, finished partitions.
-template <typename K>
-__global__ void __launch_bounds__(kThreads, 2)
+template <typename K, int NBITS>
+__global__ void __launch_bounds__(kPassThreads, 2)
     onesweep_kernel(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                     const uint32_t* __restrict__ ref_counter, uint32_t capacity, int word,
@@ -168,7 +171,8 @@ __global__ void __launch_bounds__(kThreads, 2)
                     uint32_t* __restrict__ part_counter, uint32_t* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr size_t kBuf = part_buf_bytes<K>();
-  uint32_t* s_whist = reinterpret_cast<uint32_t*>(smem + 2 * kBuf);  // [kWarps][256]
+  // [kWarps][256] per-warp digit counts, then exclusive offsets (<= 4096)
+  uint16_t* s_whist = reinterpret_cast<uint16_t*>(smem + 2 * kBuf);
   __shared__ uint32_t s_bucket[kRadixBins], s_dstart[kRadixBins], s_dest[kRadixBins];
   __shared__ uint32_t s_wsum[kWarps];
   __shared__ uint32_t s_next;
@@ -177,6 +181,9 @@ __global__ void __launch_bounds__(kThreads, 2)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t R = live_refs(ref_counter, capacity);
   const uint32_t num_parts = (R + kPart - 1) / kPart;
+  // digits are NBITS wide; the all-ones sentinel of the tail items maps to
+  // the largest digit and ranks after every real item of it
+  constexpr uint32_t kDigitMask = NBITS >= 8 ? 0xffu : ((1u << NBITS) - 1u);
 
   auto issue = [&](uint32_t part, int b) {  // thread 0 only
     unsigned char* buf = smem + b * kBuf;
@@ -186,8 +193,12 @@ __global__ void __launch_bounds__(kThreads, 2)
     bulk_g2s(buf + kb, vals_in + (size_t)part * kPart, vb, &s_bar[b]);
   };
 
+  const bool digit_thread = tid < kRadixBins;  // threads 0..255 own one digit each
   // global bucket bases of this digit place
-  s_bucket[tid] = block_exclusive_256(__ldg(hist + tid), s_wsum);
+  {
+    const uint32_t bb = block_exclusive_256(digit_thread ? __ldg(hist + tid) : 0u, s_wsum);
+    if (digit_thread) s_bucket[tid] = bb;
+  }
   if (tid == 0) {
     mbar_init(&s_bar[0], 1);
     mbar_init(&s_bar[1], 1);
@@ -212,7 +223,7 @@ __global__ void __launch_bounds__(kThreads, 2)
         issue(nxt, b ^ 1);
       }
     }
-    for (int k = tid; k < kWarps * kRadixBins; k += kThreads) s_whist[k] = 0u;
+    for (int k = tid; k < kWarps * kRadixBins; k += kPassThreads) s_whist[k] = 0u;
     K* s_keys = reinterpret_cast<K*>(smem + b * kBuf);
     uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + b * kBuf + kPart * sizeof(K));
     const bool landed = mbar_wait(&s_bar[b], b ? phase1 : phase0);
@@ -238,38 +249,40 @@ __global__ void __launch_bounds__(kThreads, 2)
         key[i] = s_keys[loc];
         val[i] = s_vals[loc];
       } else {
-        key[i] = KeyOps<K>::sentinel();  // digit 255, ranked last
+        key[i] = KeyOps<K>::sentinel();  // largest digit, ranked last
         val[i] = 0u;
       }
     }
     // ---- stable rank within the warp ----
-    uint32_t* wh = s_whist + warp * kRadixBins;
+    uint16_t* wh = s_whist + warp * kRadixBins;
     const uint32_t lt = lanemask_lt();
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
-      const uint32_t d = KeyOps<K>::digit(key[i], word, shift);
-      const uint32_t peers = match_digit8(d);
+      const uint32_t d = KeyOps<K>::digit(key[i], word, shift) & kDigitMask;
+      const uint32_t peers = match_digit<NBITS>(d);
       const uint32_t prior = wh[d];
       __syncwarp();
-      if ((__ffs(peers) - 1) == lane) wh[d] = prior + __popc(peers);
+      if ((__ffs(peers) - 1) == lane) wh[d] = (uint16_t)(prior + __popc(peers));
       __syncwarp();
       dr[i] = d | ((prior + __popc(peers & lt)) << 8);
     }
     __syncthreads();  // histograms complete; every item read out of the buffer
 
     // ---- per digit (thread = digit): warp offsets, partition totals ----
-    uint32_t run = 0;
-#pragma unroll
-    for (int w = 0; w < kWarps; ++w) {
-      const uint32_t t = s_whist[w * kRadixBins + tid];
-      s_whist[w * kRadixBins + tid] = run;
-      run += t;
-    }
-    const uint32_t pub = (tid == kRadixBins - 1) ? run - (kPart - count) : run;
+    uint32_t run = 0, pub = 0;
     uint32_t* st = status + (size_t)part * kRadixBins + tid;
-    st_relaxed_u32(st, ((part == 0 ? kFlagInc : kFlagAgg) << 30) | pub);
+    if (digit_thread) {
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w) {
+        const uint32_t t = s_whist[w * kRadixBins + tid];
+        s_whist[w * kRadixBins + tid] = (uint16_t)run;
+        run += t;
+      }
+      pub = ((uint32_t)tid == kDigitMask) ? run - (kPart - count) : run;
+      st_relaxed_u32(st, ((part == 0 ? kFlagInc : kFlagAgg) << 30) | pub);
+    }
     const uint32_t dstart = block_exclusive_256(run, s_wsum);  // includes a barrier
-    s_dstart[tid] = dstart;
+    if (digit_thread) s_dstart[tid] = dstart;
     __syncthreads();
 
     // ---- reorder the partition in place ----
@@ -284,7 +297,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     // ---- decoupled look-back, one thread per digit ----
     uint32_t excl = 0;
     bool ok = true;
-    if (part > 0) {
+    if (digit_thread && part > 0) {
       for (int pp = (int)part - 1; pp >= 0; --pp) {
         const uint32_t* ps = status + (size_t)pp * kRadixBins + tid;
         uint32_t w = ld_relaxed_u32(ps);
@@ -303,13 +316,13 @@ __global__ void __launch_bounds__(kThreads, 2)
       }
       st_relaxed_u32(st, (kFlagInc << 30) | ((excl + pub) & kValueMask));
     }
-    s_dest[tid] = s_bucket[tid] + excl - dstart;
+    if (digit_thread) s_dest[tid] = s_bucket[tid] + excl - dstart;
     const int all_ok = __syncthreads_and(ok);
     if (all_ok) {
       // ---- write each digit run contiguously ----
-      for (uint32_t j = tid; j < count; j += kThreads) {
+      for (uint32_t j = tid; j < count; j += kPassThreads) {
         const K k = s_keys[j];
-        const uint32_t dst = s_dest[KeyOps<K>::digit(k, word, shift)] + j;
+        const uint32_t dst = s_dest[KeyOps<K>::digit(k, word, shift) & kDigitMask] + j;
         if (dst < R) {
           keys_out[dst] = k;
           vals_out[dst] = s_vals[j];
@@ -325,28 +338,49 @@ __global__ void __launch_bounds__(kThreads, 2)
   }
 }
 
-template <typename K>
-int& blocks_per_sm() {
-  static int v = 0;
-  return v;
-}
-
-template <typename K>
+template <typename K, int NBITS>
 cudaError_t onesweep_setup(int* per_sm) {
-  int& v = blocks_per_sm<K>();
+  static int v = 0;  // per process: the library drives one device
   if (v == 0) {
-    cudaError_t e = cudaFuncSetAttribute(onesweep_kernel<K>,
+    cudaError_t e = cudaFuncSetAttribute(onesweep_kernel<K, NBITS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)pass_smem<K>());
     if (e != cudaSuccess) return e;
     int n = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, onesweep_kernel<K>, kThreads,
-                                                      pass_smem<K>());
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, onesweep_kernel<K, NBITS>,
+                                                      kPassThreads, pass_smem<K>());
     if (e != cudaSuccess) return e;
     v = n > 0 ? n : 1;
   }
   *per_sm = v;
   return cudaSuccess;
+}
+
+// One pass, with the ballot count fitted to the digit's width.
+template <typename K>
+cudaError_t launch_pass(int nbits, const K* kin, const uint32_t* vin, K* kout, uint32_t* vout,
+                        const uint32_t* ref_counter, uint32_t capacity, int word, int shift,
+                        const uint32_t* hist, uint32_t* status, uint32_t* part_counter,
+                        uint32_t* err, int sm_count, size_t parts_cap, cudaStream_t s) {
+  int per_sm = 0;
+  cudaError_t e;
+#define GS3D_PASS(NB)                                                                        \
+  e = onesweep_setup<K, NB>(&per_sm);                                                       \
+  if (e != cudaSuccess) return e;                                                           \
+  onesweep_kernel<K, NB><<<(int)std::min<size_t>((size_t)sm_count * per_sm, parts_cap),      \
+                           kPassThreads, pass_smem<K>(), s>>>(kin, vin, kout, vout,          \
+                                                              ref_counter, capacity, word,   \
+                                                              shift, hist, status,           \
+                                                              part_counter, err);            \
+  break;
+  switch (nbits <= 2 ? 2 : nbits <= 4 ? 4 : nbits <= 6 ? 6 : 8) {
+    case 2: GS3D_PASS(2)
+    case 4: GS3D_PASS(4)
+    case 6: GS3D_PASS(6)
+    default: GS3D_PASS(8)
+  }
+#undef GS3D_PASS
+  return cudaGetLastError();
 }
 
 template <typename K>
@@ -382,9 +416,7 @@ cudaError_t run_passes(const SortPlan& plan, const uint32_t* ref_counter, uint32
                        K* keys_a, uint32_t* vals_a, K* keys_b, uint32_t* vals_b,
                        uint32_t* status, uint32_t* g_hist, uint32_t* part_counters,
                        uint32_t* err, bool hist_ready, int sm_count, cudaStream_t s) {
-  int per_sm = 0;
-  cudaError_t e = onesweep_setup<K>(&per_sm);
-  if (e != cudaSuccess) return e;
+  cudaError_t e = cudaSuccess;
   const size_t parts_cap = ((size_t)capacity + kPart - 1) / kPart + 1;
   const size_t stride = parts_cap * kRadixBins;
   PassDev pd{};
@@ -399,14 +431,14 @@ cudaError_t run_passes(const SortPlan& plan, const uint32_t* ref_counter, uint32
     e = cudaMemsetAsync(status, 0, stride * plan.passes * sizeof(uint32_t), s);
   }
   if (e != cudaSuccess) return e;
-  const int grid = (int)std::min<size_t>((size_t)sm_count * per_sm, parts_cap);
   for (int p = 0; p < plan.passes; ++p) {
     const bool even = (p % 2) == 0;
-    onesweep_kernel<K><<<grid, kThreads, pass_smem<K>(), s>>>(
-        even ? keys_a : keys_b, even ? vals_a : vals_b, even ? keys_b : keys_a,
-        even ? vals_b : vals_a, ref_counter, capacity, plan.word[p], plan.shift[p],
-        g_hist + (size_t)p * kRadixBins, status + (size_t)p * stride, part_counters + p, err);
-    e = cudaGetLastError();
+    const int nbits = plan.nbits[p] > 0 ? plan.nbits[p] : 8;
+    e = launch_pass<K>(nbits, even ? keys_a : keys_b, even ? vals_a : vals_b,
+                       even ? keys_b : keys_a, even ? vals_b : vals_a, ref_counter, capacity,
+                       plan.word[p], plan.shift[p], g_hist + (size_t)p * kRadixBins,
+                       status + (size_t)p * stride, part_counters + p, err, sm_count, parts_cap,
+                       s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -420,6 +452,7 @@ SortPlan make_sort_plan(uint32_t num_tiles) {
   for (int s = 0; s < 32; s += 8) {  // depth bits (lo word)
     p.word[n] = 1;
     p.shift[n] = s;
+    p.nbits[n] = 8;
     ++n;
   }
   const uint32_t max_tile = num_tiles > 0 ? num_tiles - 1 : 0;
@@ -427,6 +460,7 @@ SortPlan make_sort_plan(uint32_t num_tiles) {
   for (int s = 0; s < bits; s += 8) {  // tile-id bits (hi word)
     p.word[n] = 0;
     p.shift[n] = s;
+    p.nbits[n] = bits - s < 8 ? bits - s : 8;  // the top digit may be narrower
     ++n;
   }
   p.passes = n;
@@ -481,6 +515,7 @@ cudaError_t launch_sort_depth_keys(const uint32_t* count, uint32_t capacity, uin
   for (int p = 0; p < 4; ++p) {
     plan.word[p] = 1;
     plan.shift[p] = 8 * p;
+    plan.nbits[p] = 8;
   }
   return run_passes<uint32_t>(plan, count, capacity, keys_a, vals_a, keys_b, vals_b, status,
                               g_hist, part_counters, err, false, sm_count, s);
