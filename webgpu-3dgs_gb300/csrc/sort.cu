@@ -41,6 +41,7 @@ constexpr int kItems = 8;
 constexpr uint32_t kPart = kPassThreads * kItems;  // 4096 keys per partition
 constexpr uint32_t kFlagAgg = 1u, kFlagInc = 2u;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
+constexpr int kLookback = 8;  // predecessor status words fetched per look-back step
 
 template <typename K>
 struct KeyOps;
@@ -298,21 +299,33 @@ __global__ void __launch_bounds__(kPassThreads, 2)
     uint32_t excl = 0;
     bool ok = true;
     if (digit_thread && part > 0) {
-      for (int pp = (int)part - 1; pp >= 0; --pp) {
-        const uint32_t* ps = status + (size_t)pp * kRadixBins + tid;
-        uint32_t w = ld_relaxed_u32(ps);
-        uint32_t spins = 0;
-        while ((w >> 30) == 0u) {
-          if (++spins > kSpinLimit) break;
-          if (spins > 16) __nanosleep(32);
-          w = ld_relaxed_u32(ps);
+      // walk back a window of kLookback predecessors per step: their status
+      // words are fetched together, so one L2 round trip covers the window
+      int pp = (int)part - 1;
+      bool found = false;
+      while (!found && ok && pp >= 0) {
+        uint32_t w[kLookback];
+#pragma unroll
+        for (int k = 0; k < kLookback; ++k)
+          w[k] = (pp - k >= 0) ? ld_relaxed_u32(status + (size_t)(pp - k) * kRadixBins + tid)
+                               : (kFlagInc << 30);
+#pragma unroll
+        for (int k = 0; k < kLookback; ++k) {
+          if (found || !ok) break;
+          uint32_t spins = 0;
+          while ((w[k] >> 30) == 0u) {  // not published yet: poll this one
+            if (++spins > kSpinLimit) {
+              ok = false;
+              break;
+            }
+            if (spins > 16) __nanosleep(32);
+            w[k] = ld_relaxed_u32(status + (size_t)(pp - k) * kRadixBins + tid);
+          }
+          if (!ok) break;
+          excl += w[k] & kValueMask;
+          if ((w[k] >> 30) == kFlagInc) found = true;
         }
-        if ((w >> 30) == 0u) {
-          ok = false;
-          break;
-        }
-        excl += w & kValueMask;
-        if ((w >> 30) == kFlagInc) break;
+        pp -= kLookback;
       }
       st_relaxed_u32(st, (kFlagInc << 30) | ((excl + pub) & kValueMask));
     }
