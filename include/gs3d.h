@@ -158,7 +158,8 @@ typedef enum gs3d_buffer {
 /* GaussianSplatRenderer constructor + init (GaussianSplatRenderer.ts:331-471). */
 int gs3d_create(struct gs3d_ctx** out_ctx, const gs3d_config* cfg);
 int gs3d_destroy(struct gs3d_ctx* ctx);
-/* Human-readable text of the last failing call on this context (never NULL). */
+/* Human-readable text of the last failing call on this context (never NULL);
+ * with ctx == NULL, of the calling thread's last failing context-free call. */
 const char* gs3d_last_error(const struct gs3d_ctx* ctx);
 int gs3d_abi_version(void);
 
@@ -256,6 +257,29 @@ int gs3d_ref_count(struct gs3d_ctx* ctx, uint32_t* out_count);
 /* readTileCounts (GaussianSplatRenderer.ts:1278-1310): per-tile key counts
  * max(0, off[t+1]-off[t]); `n` must be >= tile count. */
 int gs3d_read_tile_counts(struct gs3d_ctx* ctx, uint32_t* counts, size_t n);
+
+/* ---- context-free, allocation-free scan ----------------------------------- */
+
+/* No counterpart in the reference.  Exclusive prefix scan of n u32 counts
+ * into offsets[0..n] (offsets[n] = total), the same single-pass scan as
+ * gs3d_prefix_scan, for callers that cannot let a library allocate device
+ * memory: applications whose GPU memory belongs to their own pool or caching
+ * allocator, and frame loops that must not hit the implicit device
+ * synchronisation of cudaMalloc/cudaFree.  It allocates nothing and needs no
+ * context: the look-back scratch is a fixed 256 KB device array inside the
+ * library, held by every GPU that loads it until the process exits.
+ *   - counts and offsets are device pointers owned by the caller; the call
+ *     enqueues on `stream` (a cudaStream_t, NULL = legacy default stream) on
+ *     the current device and returns without waiting;
+ *   - n may be at most 67,108,864 (2^26); larger n is rejected with
+ *     GS3D_ERR_INVALID_ARG and a message in gs3d_last_error(NULL);
+ *   - the first call on each device looks up the scratch array's device
+ *     address (set-up), so make it before any stream capture;
+ *   - every call on a device shares the one scratch array: calls whose
+ *     kernels overlap on the GPU (different streams, no ordering between
+ *     them) race and give wrong offsets; order them on one stream. */
+int gs3d_prefix_scan_noalloc(const uint32_t* counts, uint32_t* offsets, uint32_t n,
+                             void* stream);
 
 #ifdef __cplusplus
 }

@@ -45,7 +45,8 @@ def test_null_arguments_are_rejected(built_lib):
     assert lib.gs3d_destroy(None) == _lib.ERR_INVALID_ARG
     assert lib.gs3d_rebin(None, None, 1, 1) == _lib.ERR_INVALID_ARG
     assert lib.gs3d_synchronize(None) == _lib.ERR_INVALID_ARG
-    assert lib.gs3d_last_error(None) == b"null context"
+    assert lib.gs3d_prefix_scan_noalloc(None, None, 4, None) == _lib.ERR_INVALID_ARG
+    assert b"null" in lib.gs3d_last_error(None)
 
 
 @pytest.mark.skipif(has_gpu(), reason="checks the no-device path")

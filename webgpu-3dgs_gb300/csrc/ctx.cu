@@ -541,7 +541,7 @@ extern "C" {
 
 int gs3d_abi_version(void) { return GS3D_ABI_VERSION; }
 
-const char* gs3d_last_error(const gs3d_ctx* c) { return c ? c->err.c_str() : "null context"; }
+const char* gs3d_last_error(const gs3d_ctx* c) { return c ? c->err.c_str() : noalloc_last_error(); }
 
 int gs3d_create(gs3d_ctx** out, const gs3d_config* cfg) {
   if (!out) return GS3D_ERR_INVALID_ARG;

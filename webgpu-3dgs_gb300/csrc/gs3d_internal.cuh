@@ -209,6 +209,8 @@ cudaError_t launch_scan(const uint32_t* counts, const uint32_t* gather, uint32_t
                         uint32_t n, unsigned long long* status, uint32_t* tile_counter,
                         uint32_t epoch, uint32_t* total_out, uint32_t* err, cudaStream_t s);
 size_t scan_status_words(uint32_t n);
+// Message of the calling thread's last failing context-free call.
+const char* noalloc_last_error();
 // Emit in splat order (the reference's emit_tile_refs, one view).
 cudaError_t launch_emit(const FrameUniforms* d_frame, uint32_t n,
                         const gs3d_projected_splat* proj, const uint32_t* offsets,

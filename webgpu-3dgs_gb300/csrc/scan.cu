@@ -49,11 +49,15 @@ __global__ void __launch_bounds__(kThreads)
   const uint32_t num_tiles = (n + kTile - 1) / kTile;
   const size_t base = (size_t)tile * kTile + (size_t)threadIdx.x * kItems;
 
+  // 128-bit accesses need 16-byte aligned buffers (caller-provided pointers
+  // may be offset); otherwise the scalar path is taken
+  const bool vec_in = (reinterpret_cast<uintptr_t>(in) & 15u) == 0;
+  const bool vec_out = (reinterpret_cast<uintptr_t>(out) & 15u) == 0;
   uint32_t v[kItems];
   if (gather != nullptr) {  // counts read through a permutation (fused rebin)
 #pragma unroll
     for (int k = 0; k < kItems; ++k) v[k] = (base + k < n) ? __ldg(in + __ldg(gather + base + k)) : 0u;
-  } else if (base + kItems <= n) {
+  } else if (vec_in && base + kItems <= n) {
     const uint4 a = __ldg(reinterpret_cast<const uint4*>(in + base));
     const uint4 b = __ldg(reinterpret_cast<const uint4*>(in + base) + 1);
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
@@ -141,7 +145,7 @@ __global__ void __launch_bounds__(kThreads)
     o[k] = run;
     run += v[k];
   }
-  if (base + kItems <= n) {
+  if (vec_out && base + kItems <= n) {
     reinterpret_cast<uint4*>(out + base)[0] = make_uint4(o[0], o[1], o[2], o[3]);
     reinterpret_cast<uint4*>(out + base)[1] = make_uint4(o[4], o[5], o[6], o[7]);
   } else {

@@ -106,6 +106,7 @@ SIGNATURES = {
     "gs3d_copy_buffer_async": ([_P, _I, _P, _SZ], _I),
     "gs3d_ref_count": ([_P, C.POINTER(_U32)], _I),
     "gs3d_read_tile_counts": ([_P, _P, _SZ], _I),
+    "gs3d_prefix_scan_noalloc": ([_P, _P, _U32, _P], _I),
 }
 
 _lib = None
