@@ -314,7 +314,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--views", type=int, default=64)
-    ap.add_argument("--batch", type=int, default=16, help="views per batched rebin")
+    ap.add_argument("--batch", type=int, default=8, help="views per batched rebin")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -99,6 +99,7 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ uint32_t s_off[kThreads + 1];
   __shared__ uint32_t s_tminx[kThreads], s_tminy[kThreads], s_w[kThreads], s_cnt[kThreads];
   __shared__ uint32_t s_lo[kThreads], s_id[kThreads], s_tx[kThreads], s_tb[kThreads];
+  __shared__ float s_winv[kThreads];
   __shared__ uint32_t s_hist[TP > 0 ? TP : 1][kRadixBins];
 
   const uint32_t total = *ref_counter;
@@ -126,6 +127,7 @@ __global__ void __launch_bounds__(kThreads)
     s_id[threadIdx.x] = id;
     s_tx[threadIdx.x] = __ldg(&views[v].f.tile_count[0]);
     s_tb[threadIdx.x] = __ldg(&views[v].f.tile_base);
+    s_winv[threadIdx.x] = 1.0f / (float)w;
   }
   const uint32_t last = min(n, first + kThreads);
   if (threadIdx.x == 0) s_off[last - first] = __ldg(sorted_offsets + last);
@@ -150,8 +152,11 @@ __global__ void __launch_bounds__(kThreads)
       }
       const uint32_t k = j - s_off[lo];
       if (k < s_cnt[lo]) {
+        // row = floor(k / w) by a float reciprocal: exact while k + w < 2^22
+        // (k < w * h <= tiles of one view)
         const uint32_t w = s_w[lo];
-        tile = s_tb[lo] + (s_tminy[lo] + k / w) * s_tx[lo] + s_tminx[lo] + k % w;
+        const uint32_t row = (uint32_t)(((float)k + 0.5f) * s_winv[lo]);
+        tile = s_tb[lo] + (s_tminy[lo] + row) * s_tx[lo] + s_tminx[lo] + (k - row * w);
         keys[j] = make_uint2(tile, s_lo[lo]);
         values[j] = s_id[lo];
       } else {

@@ -81,12 +81,14 @@ __device__ __forceinline__ void prepare(SplatStage& s) {
 // rasterize_tiles.wgsl:81-98 for one (pixel, splat) pair, branch-free: a
 // skipped splat contributes alpha = 0, which leaves C and T bit-unchanged.
 // Returns true when the pixel terminates at this splat.
+template <bool EARLY_OUT>
 __device__ __forceinline__ bool blend_one(float pfx, float pfy, const SplatStage& s, Pixel& p,
                                           bool live) {
   const float4 a = s.a, b = s.b;
   const float dx = pfx - a.x;
   const float dy = pfy - a.y;
   const float d2 = fmaf(dx, dx, dy * dy);
+  if (EARLY_OUT && !(d2 <= a.z)) return false;  // outside the radius: alpha would be 0
   const float Q = fmaf(b.x * dx, dx, fmaf(b.y * dx, dy, b.z * dy * dy));  // = -power * log2(e)
   const float alpha = fminf(0.99f, a.w * ex2_approx(-Q));
   const bool ok = live && (d2 <= a.z) && (Q >= 0.0f) && (alpha >= 1.0f / 255.0f);
@@ -203,7 +205,7 @@ __device__ void raster_tile_plain(const RasterArgs& a, const TileGeom& g, SplatS
     __syncthreads();
     if (!done) {
       for (uint32_t j = 0; j < cnt; ++j) {
-        if (blend_one(pfx, pfy, cur[j], p, true)) {
+        if (blend_one<true>(pfx, pfy, cur[j], p, true)) {
           done = true;
           used = bi * nt + j + 1;
           break;
@@ -282,7 +284,7 @@ __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, Splat
         while (mask) {
           const uint32_t b = __ffs(mask) - 1;
           mask &= mask - 1;
-          if (blend_one(pfx, pfy, cur[k0 + b], p, !done)) {
+          if (blend_one<false>(pfx, pfy, cur[k0 + b], p, !done)) {
             done = true;
             used = bi * nt + k0 + b + 1;
           }
