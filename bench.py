@@ -158,6 +158,16 @@ def run_ours(args, rank, world):
                               ptr(data.sphericalHarmonics), 3, 0))
     cam_structs = [camera_struct(u) for u in cams]
 
+    # cost model of the learned schedule, behind its gate (else key counts)
+    from gs3d import learned
+    mp, mmean, mstd, mmetrics, mbound = learned.load(
+        ROOT / "webgpu-3dgs_gb300" / "gs3d" / "cost_mlp_c1.npz")
+    use_learned = learned.gate(mmetrics, mbound)
+    f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    mp, mmean, mstd = f32(mp), f32(mmean), f32(mstd)
+    check(lib.gs3d_set_cost_model(ctx, ptr(mp), ptr(mmean), ptr(mstd)))
+    batched_schedule = _lib.SCHEDULE_LEARNED if use_learned else _lib.SCHEDULE_KEY_COUNT
+
     # first pass: size the key buffers (grow on overflow) and record ref counts
     refs = []
     for cs in cam_structs:
@@ -189,11 +199,12 @@ def run_ours(args, rank, world):
             for cs in cam_structs:
                 check(lib.gs3d_rebin(ctx, C.byref(cs), WIDTH, HEIGHT))
 
-    def timed(path: str):
+    def timed(path: str, schedule=None):
         flags = _lib.FLAG_STAGE_TIMING | (_lib.FLAG_STAGEWISE_REBIN if path == "stagewise" else 0)
         check(lib.gs3d_set_flags(ctx, flags))
-        check(lib.gs3d_set_schedule(ctx, _lib.SCHEDULE_KEY_COUNT if path == "batched"
-                                    else _lib.SCHEDULE_ROW_MAJOR))
+        if schedule is None:
+            schedule = batched_schedule if path == "batched" else _lib.SCHEDULE_ROW_MAJOR
+        check(lib.gs3d_set_schedule(ctx, schedule))
         for _ in range(3):  # size the key buffers for this path's batch
             run_step(path)
             rc = lib.gs3d_synchronize(ctx)
@@ -233,6 +244,13 @@ def run_ours(args, rank, world):
     batched_ms, batched_stages, clocks = timed("batched")
     fused_ms, fused_stages, _ = timed("fused")
     stagewise_ms, stagewise_stages, _ = timed("stagewise")
+    # the raster under each work order (single-view fused path); images are identical
+    sched_raster = {}
+    for name, sc in (("row_major", _lib.SCHEDULE_ROW_MAJOR), ("key_count", _lib.SCHEDULE_KEY_COUNT),
+                     ("learned", _lib.SCHEDULE_LEARNED)):
+        ms_, st_, _ = timed("fused", sc)
+        sched_raster[name] = {"raster_ms": round(st_["rasterize-tiles"][0], 4),
+                              "views_per_s": round(views * world / (ms_ * 1e-3), 1)}
     views = args.steps * len(cam_structs)
 
     # ---- e2e: public entry point, host camera in, pinned host image out ----
@@ -275,8 +293,9 @@ def run_ours(args, rank, world):
     hbm = [s for s in batched_roof if s != "rasterize-tiles"]
     dom = max(hbm, key=lambda s: batched_roof[s]["ms"])
     # kernels of one batched rebin: preprocess, depth sort (histogram + 4 passes), scan, emit,
-    # tile-digit passes, identify, schedule (keys + histogram + 2 passes), raster
-    launches_per_batch = 1 + 5 + 1 + 1 + batch_tile_passes + 1 + 4 + 1
+    # tile-digit passes, identify, schedule (features + MLP + keys + histogram + 2 passes
+    # for the learned one; keys + histogram + 2 passes for key counts), raster
+    launches_per_batch = 1 + 5 + 1 + 1 + batch_tile_passes + 1 + (6 if use_learned else 4) + 1
     return {
         "value": views * world / (batched_ms * 1e-3), "ms_per_step": batched_ms / args.steps,
         "views": views, "per_stage": batched_roof, "dominant": dom, "peak": peak,
@@ -288,8 +307,41 @@ def run_ours(args, rank, world):
         "e2e_value": views * world / (e2e_ms * 1e-3), "e2e_wall_value": views / e2e_wall,
         "h2d": 288 * len(cam_structs), "d2h": img_bytes * len(cam_structs),
         "launches_per_step": launches_per_batch * len(batches),
+        "schedules": sched_raster, "learned_active": use_learned,
+        "cost_model": {k: round(v, 4) for k, v in mmetrics.items()},
         "tile_passes_batched": batch_tile_passes,
     }
+
+
+def profile_run(args):
+    """Renders the workload through the batched path for a profiler: each
+    step = ceil(views / batch) launch sequences; nothing is timed."""
+    from gs3d import _lib
+    from gs3d.camera import camera_struct
+    lib = _lib.load()
+    ctx = C.c_void_p()
+    if lib.gs3d_create(C.byref(ctx), None) != 0:
+        raise RuntimeError("gs3d_create failed")
+    data, cams = make_workload(args.views)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    assert lib.gs3d_set_splats(ctx, data.splatCount, ptr(data.positions), ptr(data.scales),
+                               ptr(data.rotations), ptr(data.colors),
+                               ptr(data.sphericalHarmonics), 3, 0) == 0
+    assert lib.gs3d_set_schedule(ctx, _lib.SCHEDULE_KEY_COUNT) == 0
+    B = args.batch
+    for step in range(args.profile):
+        for b0 in range(0, len(cams), B):
+            arr = (_lib.View_t * min(B, len(cams) - b0))()
+            for i in range(len(arr)):
+                arr[i].camera = camera_struct(cams[b0 + i])
+                arr[i].width, arr[i].height = WIDTH, HEIGHT
+            for _ in range(3):
+                assert lib.gs3d_rebin_batch(ctx, C.cast(arr, C.c_void_p), len(arr)) == 0
+                rc = lib.gs3d_synchronize(ctx)
+                if rc != _lib.ERR_CAPACITY:
+                    break
+            assert rc == 0, lib.gs3d_last_error(ctx)
+    lib.gs3d_destroy(ctx)
 
 
 def cpu_view_seconds(n_views=1, threads=0):
@@ -317,6 +369,9 @@ def main():
     ap.add_argument("--batch", type=int, default=8, help="views per batched rebin")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", type=int, default=0, metavar="STEPS",
+                    help="profiling run: render STEPS batched steps of --views views and exit "
+                         "(no timing, no JSON)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -341,6 +396,9 @@ def main():
         }))
         return
 
+    if args.profile:
+        profile_run(args)
+        return
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
@@ -358,12 +416,15 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": WORKLOAD,
-                       "path": f"batched fused rebin, {args.batch} views per launch sequence, "
-                               "key-count raster schedule",
+                       "path": f"batched fused rebin, {args.batch} views per launch sequence",
                        "views_per_step": args.views, "l2": "inputs larger than L2 (no flush)",
                        "mean_refs_per_view": res["mean_refs"],
                        "tile_digit_passes": res["tile_passes_batched"],
                        "single_view_fused_views_per_s": res["fused_value"],
+                       "raster_schedule": "learned (cost MLP)" if res["learned_active"]
+                                          else "key count (cost MLP gated off)",
+                       "schedules_single_view": res["schedules"],
+                       "cost_model_heldout": res["cost_model"],
                        "plain_stagewise_views_per_s": res["stagewise_value"]},
             "roofline": {"bound": "hbm", "kernel": res["dominant"], "achieved": dom["gbs"],
                          "peak": res["peak"], "unit": "GB/s", "frac": dom["frac_hbm"],

@@ -129,6 +129,16 @@ typedef struct gs3d_view_info {
 /* Raster work order (the persistent raster CTAs pull tiles from a queue). */
 #define GS3D_SCHEDULE_ROW_MAJOR 0u  /* the reference's dispatch order          */
 #define GS3D_SCHEDULE_KEY_COUNT 1u  /* decreasing key count (longest first)    */
+#define GS3D_SCHEDULE_LEARNED   2u  /* decreasing cost predicted by the cost
+                                       MLP (gs3d_set_cost_model)               */
+
+/* Cost MLP (extension): 16 tile features -> 64 -> 64 -> 1, ReLU, predicting
+ * log(1 + raster cost), the cost being the splats a tile's CTA iterates
+ * before its last pixel terminates.  Parameters are f32, in this order:
+ * W1[64][16], b1[64], W2[64][64], b2[64], w3[64], b3. */
+#define GS3D_MLP_FEATURES 16
+#define GS3D_MLP_HIDDEN   64
+#define GS3D_MLP_PARAMS   (64 * 16 + 64 + 64 * 64 + 64 + 64 + 1)
 
 /* Named device buffers (BufferManager names, GaussianSplatRenderer.ts:338-465). */
 typedef enum gs3d_buffer {
@@ -226,8 +236,32 @@ int gs3d_rebin_batch(struct gs3d_ctx* ctx, const gs3d_view* views, uint32_t n_vi
 int gs3d_get_view_info(struct gs3d_ctx* ctx, uint32_t view, gs3d_view_info* out);
 
 /* Selects the raster work order (GS3D_SCHEDULE_*); the image is the same
- * under every schedule. */
+ * under every schedule.  GS3D_SCHEDULE_LEARNED needs a cost model. */
 int gs3d_set_schedule(struct gs3d_ctx* ctx, uint32_t schedule);
+
+/* Installs the cost MLP: GS3D_MLP_PARAMS f32 parameters and the per-feature
+ * mean and standard deviation the features are normalized with (host
+ * pointers). */
+int gs3d_set_cost_model(struct gs3d_ctx* ctx, const float* params,
+                        const float* feature_mean, const float* feature_std);
+
+/* Raw features (n_tiles x 16 f32) of every tile of the last rebin and, in
+ * targets (n_tiles f32, may be NULL), log(1 + measured raster cost).
+ * memory: 0 = host pointers (blocking), 1 = device pointers (stream ordered). */
+int gs3d_tile_features(struct gs3d_ctx* ctx, float* features, float* targets,
+                       uint32_t n_tiles, int memory);
+
+/* Cost-MLP kernels on caller device buffers, enqueued on `stream` (no
+ * context): f32 training forward (acts: n x 129 = h1 | h2 | y), backward
+ * (grads += d mean((y - target)^2) / d params; zero grads first), Adam step
+ * (step >= 1), and bf16 tensor-core inference (mma.sync). */
+int gs3d_mlp_forward(const float* params, const float* x, uint32_t n, float* acts, float* y,
+                     void* stream);
+int gs3d_mlp_backward(const float* params, const float* x, const float* acts,
+                      const float* target, uint32_t n, float* grads, void* stream);
+int gs3d_mlp_adam(float* params, float* m, float* v, const float* grads, uint32_t count,
+                  float lr, float beta1, float beta2, float eps, uint32_t step, void* stream);
+int gs3d_mlp_infer(const float* params, const float* x, uint32_t n, float* y, void* stream);
 
 /* Waits for the context's stream and reports latched device errors.  After
  * GS3D_ERR_CAPACITY the key buffers have already been grown to the observed

@@ -210,3 +210,29 @@ def test_camera_module_matches_oracle(oracle):
         # by the last bits of a double cancellation
         np.testing.assert_allclose(u1[:32], u2[:32], rtol=2e-7, atol=1e-6)
         np.testing.assert_array_equal(u1[64:], u2[64:])
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The float64 cost-MLP oracle that checks the GPU training kernels."""
+    from oracle import mlp_oracle
+    from gs3d import learned
+    rng = np.random.default_rng(2)
+    p = learned.init_params(4, 0.3).astype(np.float64)
+    x, t = rng.normal(0, 1, (40, 16)), rng.normal(1, 1, 40)
+    g = mlp_oracle.grad(p, x, t)
+    loss = lambda q: np.mean((mlp_oracle.forward(q, x)[0] - t) ** 2)  # noqa: E731
+    for i in rng.choice(len(p), 60, replace=False):
+        e = np.zeros_like(p)
+        e[i] = 1e-6
+        fd = (loss(p + e) - loss(p - e)) / 2e-6
+        assert abs(fd - g[i]) <= 1e-5 * max(1.0, abs(g[i]))
+
+
+def test_learned_gate():
+    from gs3d import learned
+    good = {"mlp_mae_log": 0.2, "keycount_mae_log": 0.4, "mlp_spearman": 0.9,
+            "keycount_spearman": 0.8}
+    assert learned.gate(good)
+    assert not learned.gate({**good, "mlp_mae_log": 0.9})       # error above the bound
+    assert not learned.gate({**good, "mlp_spearman": 0.7})      # ranks worse than key count
+    assert abs(learned.spearman(np.arange(10.0), np.arange(10.0) ** 2) - 1.0) < 1e-12

@@ -78,6 +78,9 @@ struct gs3d_ctx {
   DevBuf depth_keys_a, depth_ids_a, depth_keys_b, depth_ids_b, sorted_offsets, depth_status;
   DevBuf tile_offsets, image, tile_costs;
   DevBuf sched_keys_a, sched_keys_b, sched_order_a, sched_order_b, sched_status;
+  // cost model (learned schedule)
+  bool have_model = false;
+  DevBuf model_params, model_mean, model_inv_std, tile_feats, tile_preds;
 
   // the current batch (a single-view frame is a batch of one)
   bool have_camera = false;
@@ -383,6 +386,8 @@ int set_views(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views) {
   TRY(ensure(c, c->sched_order_a, td * 4, "schedule order"));
   TRY(ensure(c, c->sched_order_b, td * 4, "schedule order"));
   TRY(ensure(c, c->sched_status, sort_status_words((uint32_t)tiles, 4) * 4, "schedule status"));
+  TRY(ensure(c, c->tile_feats, std::max<uint64_t>(tiles, 1) * kFeatures * 4, "tile features"));
+  TRY(ensure(c, c->tile_preds, std::max<uint64_t>(tiles, 1) * 4, "tile cost predictions"));
   TRY(ensure(c, c->d_views, (size_t)n_views * sizeof(ViewDesc), "view table"));
   if (c->capacity < 1) TRY(ensure_key_capacity(c, 1));
 
@@ -445,6 +450,23 @@ int raster_stage(gs3d_ctx* c, bool culled) {
   StageScope t(c, GS3D_STAGE_RASTER);
   const uint32_t* order = nullptr;
   if (c->schedule != GS3D_SCHEDULE_ROW_MAJOR && c->total_tiles > 1) {
+    if (c->schedule == GS3D_SCHEDULE_LEARNED) {
+      const uint32_t nv = (uint32_t)c->views.size();
+      CK(launch_tile_features(dviews(c), nv, c->total_tiles, c->tile_w, c->tile_h,
+                              u32(c->tile_offsets), u32(c->vals_a),
+                              static_cast<gs3d_projected_splat*>(c->proj.p),
+                              static_cast<float*>(c->model_mean.p),
+                              static_cast<float*>(c->model_inv_std.p),
+                              static_cast<float*>(c->tile_feats.p), c->stream),
+         "tile features");
+      CK(launch_mlp_infer(static_cast<float*>(c->model_params.p),
+                          static_cast<float*>(c->tile_feats.p), c->total_tiles,
+                          static_cast<float*>(c->tile_preds.p), c->stream),
+         "cost MLP inference");
+      CK(launch_learned_keys(static_cast<float*>(c->tile_preds.p), c->total_tiles,
+                             u32(c->sched_keys_a), u32(c->sched_order_a), c->stream),
+         "learned schedule keys");
+    }
     CK(launch_schedule(c->schedule, u32(c->tile_offsets), c->total_tiles,
                        &dviews(c)->batch_tiles, u32(c->sched_keys_a), u32(c->sched_order_a), u32(c->sched_keys_b),
                        u32(c->sched_order_b), u32(c->sched_status), ctrl_of(c), c->sm_count,
@@ -616,7 +638,8 @@ int gs3d_destroy(gs3d_ctx* c) {
                     &c->depth_keys_b,  &c->depth_ids_b,   &c->sorted_offsets, &c->depth_status,
                     &c->tile_offsets,  &c->image,         &c->tile_costs,    &c->sched_keys_a,
                     &c->sched_keys_b,  &c->sched_order_a, &c->sched_order_b, &c->sched_status,
-                    &c->d_views,       &c->ctrl};
+                    &c->d_views,       &c->ctrl,          &c->model_params,  &c->model_mean,
+                    &c->model_inv_std, &c->tile_feats,    &c->tile_preds};
   for (DevBuf* b : bufs) release(*b);
   for (int i = 0; i < kUploadSlots; ++i)
     if (c->upload_ev[i]) cudaEventDestroy(c->upload_ev[i]);
@@ -811,10 +834,96 @@ int gs3d_get_view_info(gs3d_ctx* c, uint32_t view, gs3d_view_info* out) {
 
 int gs3d_set_schedule(gs3d_ctx* c, uint32_t schedule) {
   if (!c) return GS3D_ERR_INVALID_ARG;
-  if (schedule > GS3D_SCHEDULE_KEY_COUNT)
+  if (schedule > GS3D_SCHEDULE_LEARNED)
     return fail(c, GS3D_ERR_INVALID_ARG, "unknown schedule %u", schedule);
+  if (schedule == GS3D_SCHEDULE_LEARNED && !c->have_model)
+    return fail(c, GS3D_ERR_STATE, "the learned schedule needs gs3d_set_cost_model first");
   c->schedule = schedule;
   return GS3D_OK;
+}
+
+int gs3d_set_cost_model(gs3d_ctx* c, const float* params, const float* mean, const float* std_) {
+  if (!c || !params || !mean || !std_) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
+  TRY(set_device(c));
+  float inv[kFeatures];
+  for (int k = 0; k < kFeatures; ++k) {
+    if (!(std_[k] > 0.0f)) return fail(c, GS3D_ERR_INVALID_ARG, "feature std %d is not > 0", k);
+    inv[k] = 1.0f / std_[k];
+  }
+  TRY(ensure(c, c->model_params, kMlpParams * 4, "cost model"));
+  TRY(ensure(c, c->model_mean, kFeatures * 4, "cost model"));
+  TRY(ensure(c, c->model_inv_std, kFeatures * 4, "cost model"));
+  CK(cudaStreamSynchronize(c->stream), "install cost model");
+  CK(cudaMemcpy(c->model_params.p, params, kMlpParams * 4, cudaMemcpyHostToDevice), "cost model");
+  CK(cudaMemcpy(c->model_mean.p, mean, kFeatures * 4, cudaMemcpyHostToDevice), "cost model");
+  CK(cudaMemcpy(c->model_inv_std.p, inv, kFeatures * 4, cudaMemcpyHostToDevice), "cost model");
+  c->have_model = true;
+  return GS3D_OK;
+}
+
+int gs3d_tile_features(gs3d_ctx* c, float* features, float* targets, uint32_t n_tiles,
+                       int memory) {
+  if (!c || !features) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
+  if (memory != 0 && memory != 1) return fail(c, GS3D_ERR_INVALID_ARG, "memory must be 0 or 1");
+  TRY(require_frame(c, "tile_features"));
+  if (n_tiles < c->total_tiles)
+    return fail(c, GS3D_ERR_INVALID_ARG, "room for %u tiles, the frame has %u", n_tiles,
+                c->total_tiles);
+  TRY(set_device(c));
+  float* fdst = memory ? features : static_cast<float*>(c->tile_feats.p);
+  CK(launch_tile_features(dviews(c), (uint32_t)c->views.size(), c->total_tiles, c->tile_w,
+                          c->tile_h, u32(c->tile_offsets), u32(c->vals_a),
+                          static_cast<gs3d_projected_splat*>(c->proj.p), nullptr, nullptr, fdst,
+                          c->stream),
+     "tile features");
+  float* tdst = nullptr;
+  if (targets) {
+    tdst = memory ? targets : static_cast<float*>(c->tile_preds.p);
+    CK(launch_log_costs(u32(c->tile_costs), c->total_tiles, tdst, c->stream), "tile targets");
+  }
+  if (!memory) {
+    TRY(sync_and_check(c));
+    CK(cudaMemcpy(features, fdst, (size_t)c->total_tiles * kFeatures * 4, cudaMemcpyDeviceToHost),
+       "features copy-out");
+    if (targets)
+      CK(cudaMemcpy(targets, tdst, (size_t)c->total_tiles * 4, cudaMemcpyDeviceToHost),
+         "targets copy-out");
+  }
+  return GS3D_OK;
+}
+
+int gs3d_mlp_forward(const float* params, const float* x, uint32_t n, float* acts, float* y,
+                     void* stream) {
+  if (!params || !x || !acts || !y) return GS3D_ERR_INVALID_ARG;
+  return launch_mlp_forward(params, x, n, acts, y, static_cast<cudaStream_t>(stream)) ==
+                 cudaSuccess
+             ? GS3D_OK
+             : GS3D_ERR_CUDA;
+}
+
+int gs3d_mlp_backward(const float* params, const float* x, const float* acts,
+                      const float* target, uint32_t n, float* grads, void* stream) {
+  if (!params || !x || !acts || !target || !grads) return GS3D_ERR_INVALID_ARG;
+  return launch_mlp_backward(params, x, acts, target, n, grads,
+                             static_cast<cudaStream_t>(stream)) == cudaSuccess
+             ? GS3D_OK
+             : GS3D_ERR_CUDA;
+}
+
+int gs3d_mlp_adam(float* p, float* m, float* v, const float* g, uint32_t count, float lr,
+                  float beta1, float beta2, float eps, uint32_t step, void* stream) {
+  if (!p || !m || !v || !g || step == 0) return GS3D_ERR_INVALID_ARG;
+  return launch_adam(p, m, v, g, count, lr, beta1, beta2, eps, step,
+                     static_cast<cudaStream_t>(stream)) == cudaSuccess
+             ? GS3D_OK
+             : GS3D_ERR_CUDA;
+}
+
+int gs3d_mlp_infer(const float* params, const float* x, uint32_t n, float* y, void* stream) {
+  if (!params || !x || !y) return GS3D_ERR_INVALID_ARG;
+  return launch_mlp_infer(params, x, n, y, static_cast<cudaStream_t>(stream)) == cudaSuccess
+             ? GS3D_OK
+             : GS3D_ERR_CUDA;
 }
 
 int gs3d_read_stage_times(gs3d_ctx* c, double* ms, uint32_t* n) {

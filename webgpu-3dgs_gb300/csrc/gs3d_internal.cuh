@@ -244,10 +244,33 @@ cudaError_t launch_sort_depth_keys(const uint32_t* count, uint32_t capacity, uin
 // Raster work order: tile indices sorted by decreasing expected cost
 // (schedule = GS3D_SCHEDULE_KEY_COUNT: the tile's key count), so the
 // persistent raster CTAs start the longest tiles first.
+// keys_a/order_a must already hold the keys for GS3D_SCHEDULE_LEARNED
+// (launch_learned_keys); for the key-count schedule they are computed here.
 cudaError_t launch_schedule(uint32_t schedule, const uint32_t* tile_offsets, uint32_t num_tiles,
                             const uint32_t* num_tiles_dev, uint32_t* keys_a, uint32_t* order_a,
                             uint32_t* keys_b, uint32_t* order_b, uint32_t* status, Ctrl* ctrl,
                             int sm_count, cudaStream_t s);
+
+// ---- learned schedule (learned.cu) ----
+constexpr int kFeatures = 16;
+constexpr int kHidden = 64;
+constexpr int kMlpParams = kHidden * kFeatures + kHidden + kHidden * kHidden + kHidden + kHidden + 1;
+cudaError_t launch_tile_features(const ViewDesc* views, uint32_t n_views, uint32_t num_tiles,
+                                 uint32_t tile_w, uint32_t tile_h, const uint32_t* tile_offsets,
+                                 const uint32_t* values, const gs3d_projected_splat* proj,
+                                 const float* mean, const float* inv_std, float* out,
+                                 cudaStream_t s);
+cudaError_t launch_mlp_infer(const float* params, const float* x, uint32_t n, float* y,
+                             cudaStream_t s);
+cudaError_t launch_mlp_forward(const float* params, const float* x, uint32_t n, float* acts,
+                               float* y, cudaStream_t s);
+cudaError_t launch_mlp_backward(const float* params, const float* x, const float* acts,
+                                const float* target, uint32_t n, float* grads, cudaStream_t s);
+cudaError_t launch_adam(float* p, float* m, float* v, const float* g, uint32_t count, float lr,
+                        float beta1, float beta2, float eps, uint32_t step, cudaStream_t s);
+cudaError_t launch_learned_keys(const float* pred, uint32_t n, uint32_t* keys, uint32_t* ids,
+                                cudaStream_t s);
+cudaError_t launch_log_costs(const uint32_t* costs, uint32_t n, float* out, cudaStream_t s);
 
 // Emit in depth-sorted order over all splat-views of a batch (global tile
 // ids, global splat-view values) + histograms of the tile-id digit places.

@@ -8,7 +8,8 @@
 // which CTA renders a tile and when; every pixel's arithmetic is unchanged.
 //
 // Key-count schedule: expected cost = the tile's key count (the plain
-// schedule the learned one falls back to).
+// schedule the learned one falls back to).  Learned schedule: expected cost
+// = the cost MLP's prediction (learned.cu); both sort 16-bit keys.
 #include "gs3d_internal.cuh"
 
 namespace gs3d {
@@ -35,12 +36,14 @@ cudaError_t launch_schedule(uint32_t schedule, const uint32_t* tile_offsets, uin
                             const uint32_t* num_tiles_dev, uint32_t* keys_a, uint32_t* order_a,
                             uint32_t* keys_b, uint32_t* order_b, uint32_t* status, Ctrl* ctrl,
                             int sm_count, cudaStream_t s) {
-  (void)schedule;
   if (num_tiles == 0) return cudaSuccess;
-  keycount_keys_kernel<<<(num_tiles + kThreads - 1) / kThreads, kThreads, 0, s>>>(
-      tile_offsets, num_tiles, keys_a, order_a);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  cudaError_t e = cudaSuccess;
+  if (schedule == GS3D_SCHEDULE_KEY_COUNT) {
+    keycount_keys_kernel<<<(num_tiles + kThreads - 1) / kThreads, kThreads, 0, s>>>(
+        tile_offsets, num_tiles, keys_a, order_a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   e = cudaMemsetAsync(ctrl->sched_counter, 0, sizeof(ctrl->sched_counter), s);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(ctrl->sched_hist, 0, sizeof(ctrl->sched_hist), s);

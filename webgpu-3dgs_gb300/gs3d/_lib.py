@@ -73,6 +73,9 @@ class ViewInfo_t(C.Structure):
 
 SCHEDULE_ROW_MAJOR = 0
 SCHEDULE_KEY_COUNT = 1
+SCHEDULE_LEARNED = 2
+MLP_FEATURES, MLP_HIDDEN = 16, 64
+MLP_PARAMS = 64 * 16 + 64 + 64 * 64 + 64 + 64 + 1
 
 assert C.sizeof(Camera_t) == 288
 
@@ -107,6 +110,13 @@ SIGNATURES = {
     "gs3d_ref_count": ([_P, C.POINTER(_U32)], _I),
     "gs3d_read_tile_counts": ([_P, _P, _SZ], _I),
     "gs3d_prefix_scan_noalloc": ([_P, _P, _U32, _P], _I),
+    "gs3d_set_cost_model": ([_P, _P, _P, _P], _I),
+    "gs3d_tile_features": ([_P, _P, _P, _U32, _I], _I),
+    "gs3d_mlp_forward": ([_P, _P, _U32, _P, _P, _P], _I),
+    "gs3d_mlp_backward": ([_P, _P, _P, _P, _U32, _P, _P], _I),
+    "gs3d_mlp_adam": ([_P, _P, _P, _P, _U32, C.c_float, C.c_float, C.c_float, C.c_float,
+                       _U32, _P], _I),
+    "gs3d_mlp_infer": ([_P, _P, _U32, _P, _P], _I),
 }
 
 _lib = None

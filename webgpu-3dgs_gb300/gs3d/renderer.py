@@ -142,6 +142,26 @@ class GaussianSplatRenderer:
         """Raster work order: _lib.SCHEDULE_ROW_MAJOR or SCHEDULE_KEY_COUNT."""
         self._call("gs3d_set_schedule", int(schedule))
 
+    def setCostModel(self, path=None) -> bool:
+        """Loads a cost-MLP checkpoint (default: the one trained for the 3M-splat
+        1080p workload).  When its held-out error is within its bound and it
+        ranks tiles better than the key count, it is installed and the learned
+        schedule selected; otherwise the key-count schedule is selected.
+        Returns whether the learned schedule is active."""
+        from pathlib import Path
+        from . import learned
+        path = Path(path) if path else Path(__file__).with_name("cost_mlp_c1.npz")
+        params, mean, std, metrics, bound = learned.load(path)
+        if not learned.gate(metrics, bound):
+            self.setSchedule(_lib.SCHEDULE_KEY_COUNT)
+            return False
+        f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+        params, mean, std = f32(params), f32(mean), f32(std)
+        self._call("gs3d_set_cost_model", params.ctypes.data_as(C.c_void_p),
+                   mean.ctypes.data_as(C.c_void_p), std.ctypes.data_as(C.c_void_p))
+        self.setSchedule(_lib.SCHEDULE_LEARNED)
+        return True
+
     def setAlwaysRebin(self, on: bool) -> None:
         self.alwaysRebin = bool(on)
 
