@@ -91,6 +91,12 @@ typedef struct gs3d_config {
 /* Records a CUDA event pair around every stage on the context's stream;
  * gs3d_read_stage_times returns the accumulated device time per stage. */
 #define GS3D_FLAG_STAGE_TIMING    2u
+/* Fused rebins (gs3d_rebin, gs3d_rebin_batch) run as a CUDA graph: the
+ * first rebin of a batch layout (views, scenes, sizes, tile size, schedule,
+ * buffer allocations) runs once eagerly and is captured; later rebins of the
+ * same layout only rewrite the view table and replay the graph.  Stage
+ * timing events are not recorded in graph mode. */
+#define GS3D_FLAG_CUDA_GRAPH      4u
 
 /* Stage indices of gs3d_read_stage_times (the reference's profiler labels,
  * GaussianSplatRenderer.ts:1144-1260, plus the fused path's depth sort). */

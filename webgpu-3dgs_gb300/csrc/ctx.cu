@@ -96,6 +96,17 @@ struct gs3d_ctx {
 
   DevBuf ctrl;
   uint32_t* h_word = nullptr;  // pinned scratch for small reads
+  uint64_t alloc_gen = 0;      // bumped by every device (re)allocation
+
+  // CUDA-graph replay of the fused rebin (GS3D_FLAG_CUDA_GRAPH)
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uint64_t> sig;     // batch signature the graph was captured for
+    ViewDesc* h_views = nullptr;   // pinned view table read by the graph's copy node
+    size_t cap = 0;
+    cudaEvent_t copied = nullptr;  // recorded after each replay (pinned slot reuse)
+    void* result_keys = nullptr;   // buffer holding the sorted keys after a replay
+  } graph;
 
   // optional stage timing (GS3D_FLAG_STAGE_TIMING)
   struct Pending {
@@ -165,6 +176,7 @@ int ensure(gs3d_ctx* c, DevBuf& b, size_t bytes, const char* name) {
   }
   b.p = p;
   b.bytes = bytes;
+  ++c->alloc_gen;
   return GS3D_OK;
 }
 
@@ -315,7 +327,7 @@ int upload_scene(gs3d_ctx* c, SceneBufs& sc, uint32_t n, const float* positions,
 
 // Builds the batch layout on the host, sizes every buffer for it and uploads
 // the view table through a pinned ring slot (stream ordered).
-int set_views(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views) {
+int set_views(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views, bool upload = true) {
   if (n_views == 0 || !views) return fail(c, GS3D_ERR_INVALID_ARG, "empty view list");
   std::vector<ViewDesc> vds(n_views, ViewDesc{});
   std::vector<gs3d_view_info> infos(n_views, gs3d_view_info{});
@@ -391,6 +403,17 @@ int set_views(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views) {
   TRY(ensure(c, c->d_views, (size_t)n_views * sizeof(ViewDesc), "view table"));
   if (c->capacity < 1) TRY(ensure_key_capacity(c, 1));
 
+  if (!upload) {  // the caller uploads the table (CUDA-graph replay)
+    c->views.swap(vds);
+    c->info.swap(infos);
+    c->total_splats = (uint32_t)splats;
+    c->total_tiles = (uint32_t)tiles;
+    c->total_pixels = pixels;
+    c->total_blocks = (uint32_t)blocks;
+    c->max_sh = max_sh;
+    c->have_camera = true;
+    return GS3D_OK;
+  }
   if (n_views > c->upload_cap) {  // grow the pinned ring (idle stream first)
     CK(cudaStreamSynchronize(c->stream), "upload ring resize");
     if (c->h_upload) cudaFreeHost(c->h_upload);
@@ -520,6 +543,9 @@ int fused_rebin(gs3d_ctx* c) {
   c->scan_epoch = (c->scan_epoch % ((1u << 30) - 1)) + 1;
   {
     StageScope t(c, GS3D_STAGE_SCAN);
+    // cleared every rebin: a graph replay reuses the captured epoch
+    CK(cudaMemsetAsync(c->scan_status.p, 0, scan_status_words(c->total_splats) * 8, c->stream),
+       "clear scan status");
     CK(launch_scan(u32(c->counts), u32(c->depth_ids_a), u32(c->sorted_offsets), c->total_splats,
                    static_cast<unsigned long long*>(c->scan_status.p), &k->scan_tile_counter,
                    c->scan_epoch, u32(c->ref_counter), &k->error, c->stream),
@@ -555,6 +581,85 @@ int fused_rebin(gs3d_ctx* c) {
        "identify_tile_ranges");
   }
   return raster_stage(c, true);
+}
+
+void destroy_graph(gs3d_ctx* c) {
+  if (c->graph.exec) cudaGraphExecDestroy(c->graph.exec);
+  c->graph.exec = nullptr;
+  c->graph.sig.clear();
+}
+
+std::vector<uint64_t> graph_signature(gs3d_ctx* c) {
+  std::vector<uint64_t> sig = {c->views.size(), c->tile_w, c->tile_h, c->schedule,
+                               c->capacity, c->alloc_gen, c->max_sh,
+                               c->flags & ~GS3D_FLAG_STAGE_TIMING};
+  for (const ViewDesc& v : c->views) {
+    sig.push_back((uint64_t)(uintptr_t)v.pos);
+    sig.push_back(((uint64_t)v.f.viewport[0] << 32) | v.f.viewport[1]);
+    sig.push_back(v.f.splat_count);
+  }
+  return sig;
+}
+
+// Fused rebin through a CUDA graph: captured once per batch signature (the
+// view-table upload from a fixed pinned slot, the counter resets and every
+// kernel of the rebin), then replayed with only the pinned view table
+// rewritten.  Any reallocation or layout change re-captures.
+int graph_rebin(gs3d_ctx* c) {
+  TRY(require_frame(c, "rebin"));
+  const size_t nv = c->views.size();
+  std::vector<uint64_t> sig = graph_signature(c);
+  if (!c->graph.exec || sig != c->graph.sig) {
+    destroy_graph(c);
+    if (nv > c->graph.cap) {
+      CK(cudaStreamSynchronize(c->stream), "graph view slot");
+      if (c->graph.h_views) cudaFreeHost(c->graph.h_views);
+      c->graph.h_views = nullptr;
+      c->graph.cap = 0;
+      CK(cudaMallocHost(&c->graph.h_views, nv * sizeof(ViewDesc)), "graph view slot");
+      c->graph.cap = nv;
+    }
+    if (!c->graph.copied)
+      CK(cudaEventCreateWithFlags(&c->graph.copied, cudaEventDisableTiming), "graph event");
+    // one eager rebin first: launch configurations are cached and the key
+    // buffers sized before anything is captured
+    std::memcpy(c->graph.h_views, c->views.data(), nv * sizeof(ViewDesc));
+    CK(cudaMemcpyAsync(c->d_views.p, c->graph.h_views, nv * sizeof(ViewDesc),
+                       cudaMemcpyHostToDevice, c->stream),
+       "upload view table");
+    TRY(fused_rebin(c));
+    CK(cudaStreamSynchronize(c->stream), "graph warm-up");
+    sig = graph_signature(c);
+    const uint32_t saved_flags = c->flags;
+    c->flags &= ~GS3D_FLAG_STAGE_TIMING;  // no timing events inside the graph
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const cudaError_t ce = cudaMemcpyAsync(c->d_views.p, c->graph.h_views, nv * sizeof(ViewDesc),
+                                           cudaMemcpyHostToDevice, c->stream);
+    const int rc = ce == cudaSuccess ? fused_rebin(c) : GS3D_ERR_CUDA;
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(c->stream, &g);
+    c->flags = saved_flags;
+    if (rc != GS3D_OK || ce != cudaSuccess || ee != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      return rc != GS3D_OK ? rc : fail(c, GS3D_ERR_CUDA, "rebin graph capture failed");
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&c->graph.exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(ie, "graph instantiate");
+    c->graph.sig = sig;
+    c->graph.result_keys = c->keys_a.p;  // where a replay leaves the sorted keys
+  }
+  // the previous replay read the pinned table at its start; wait for it
+  CK(cudaEventSynchronize(c->graph.copied), "graph view slot reuse");
+  std::memcpy(c->graph.h_views, c->views.data(), nv * sizeof(ViewDesc));
+  CK(cudaGraphLaunch(c->graph.exec, c->stream), "graph launch");
+  CK(cudaEventRecord(c->graph.copied, c->stream), "graph event");
+  if (c->keys_a.p != c->graph.result_keys) {  // an eager rebin renamed the ping-pong pair
+    std::swap(c->keys_a, c->keys_b);
+    std::swap(c->vals_a, c->vals_b);
+  }
+  return GS3D_OK;
 }
 
 }  // namespace
@@ -644,6 +749,9 @@ int gs3d_destroy(gs3d_ctx* c) {
   for (int i = 0; i < kUploadSlots; ++i)
     if (c->upload_ev[i]) cudaEventDestroy(c->upload_ev[i]);
   for (auto& e : c->ev_pool) cudaEventDestroy(e);
+  destroy_graph(c);
+  if (c->graph.copied) cudaEventDestroy(c->graph.copied);
+  if (c->graph.h_views) cudaFreeHost(c->graph.h_views);
   if (c->h_upload) cudaFreeHost(c->h_upload);
   if (c->h_word) cudaFreeHost(c->h_word);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -742,6 +850,8 @@ int gs3d_prefix_scan(gs3d_ctx* c) {
      "reset scan ticket");
   c->scan_epoch = (c->scan_epoch % ((1u << 30) - 1)) + 1;  // 1 .. 2^30-1, never 0
   StageScope t(c, GS3D_STAGE_SCAN);
+  CK(cudaMemsetAsync(c->scan_status.p, 0, scan_status_words(c->total_splats) * 8, c->stream),
+     "clear scan status");
   CK(launch_scan(u32(c->counts), nullptr, u32(c->offsets), c->total_splats,
                  static_cast<unsigned long long*>(c->scan_status.p),
                  &ctrl_of(c)->scan_tile_counter, c->scan_epoch, u32(c->ref_counter),
@@ -803,8 +913,18 @@ int gs3d_rasterize_tiles(gs3d_ctx* c) {
 
 int gs3d_rebin(gs3d_ctx* c, const gs3d_camera* cam, uint32_t width, uint32_t height) {
   if (!c) return GS3D_ERR_INVALID_ARG;
-  TRY(gs3d_set_camera(c, cam, width, height));
   TRY(set_device(c));
+  if ((c->flags & GS3D_FLAG_CUDA_GRAPH) && !(c->flags & GS3D_FLAG_STAGEWISE_REBIN)) {
+    if (!cam) return fail(c, GS3D_ERR_INVALID_ARG, "null camera");
+    if (!c->have_scene) return fail(c, GS3D_ERR_STATE, "rebin: no splats set");
+    gs3d_view v{};
+    v.camera = *cam;
+    v.width = width;
+    v.height = height;
+    TRY(set_views(c, &v, 1, false));
+    return graph_rebin(c);
+  }
+  TRY(gs3d_set_camera(c, cam, width, height));
   if (!(c->flags & GS3D_FLAG_STAGEWISE_REBIN)) return fused_rebin(c);
   TRY(gs3d_preprocess(c));
   TRY(gs3d_prefix_scan(c));
@@ -819,6 +939,10 @@ int gs3d_rebin_batch(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views) {
   if (!c) return GS3D_ERR_INVALID_ARG;
   if (!c->have_scene) return fail(c, GS3D_ERR_STATE, "rebin_batch: no scene");
   TRY(set_device(c));
+  if (c->flags & GS3D_FLAG_CUDA_GRAPH) {
+    TRY(set_views(c, views, n_views, false));
+    return graph_rebin(c);
+  }
   TRY(set_views(c, views, n_views));
   return fused_rebin(c);
 }
@@ -941,7 +1065,7 @@ int gs3d_read_stage_times(gs3d_ctx* c, double* ms, uint32_t* n) {
 
 int gs3d_set_flags(gs3d_ctx* c, uint32_t flags) {
   if (!c) return GS3D_ERR_INVALID_ARG;
-  if (flags & ~(GS3D_FLAG_STAGEWISE_REBIN | GS3D_FLAG_STAGE_TIMING))
+  if (flags & ~(GS3D_FLAG_STAGEWISE_REBIN | GS3D_FLAG_STAGE_TIMING | GS3D_FLAG_CUDA_GRAPH))
     return fail(c, GS3D_ERR_INVALID_ARG, "unknown flag bits 0x%x", flags);
   c->flags = flags;
   return GS3D_OK;

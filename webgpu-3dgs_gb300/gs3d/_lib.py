@@ -28,6 +28,7 @@ STATUS_NAMES = {
 
 FLAG_STAGEWISE_REBIN = 1
 FLAG_STAGE_TIMING = 2
+FLAG_CUDA_GRAPH = 4
 STAGE_NAMES = ["preprocess-splats", "depth-sort", "prefix-scan", "emit-tile-refs", "radix-sort",
                "identify-tile-ranges", "rasterize-tiles"]
 

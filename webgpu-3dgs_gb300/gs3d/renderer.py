@@ -136,7 +136,15 @@ class GaussianSplatRenderer:
         """Selects the stage-wise rebin (the six reference stages in order)
         instead of the fused default; both give identical sorted keys,
         values, tile ranges and images."""
-        self._call("gs3d_set_flags", _lib.FLAG_STAGEWISE_REBIN if on else 0)
+        self._flags = (getattr(self, "_flags", 0) & ~_lib.FLAG_STAGEWISE_REBIN) | \
+            (_lib.FLAG_STAGEWISE_REBIN if on else 0)
+        self._call("gs3d_set_flags", self._flags)
+
+    def setCudaGraph(self, on: bool) -> None:
+        """Runs fused rebins as a captured CUDA graph, replayed per batch layout."""
+        self._flags = (getattr(self, "_flags", 0) & ~_lib.FLAG_CUDA_GRAPH) | \
+            (_lib.FLAG_CUDA_GRAPH if on else 0)
+        self._call("gs3d_set_flags", self._flags)
 
     def setSchedule(self, schedule: int) -> None:
         """Raster work order: _lib.SCHEDULE_ROW_MAJOR or SCHEDULE_KEY_COUNT."""
