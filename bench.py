@@ -331,7 +331,14 @@ def profile_run(args):
     assert lib.gs3d_set_splats(ctx, data.splatCount, ptr(data.positions), ptr(data.scales),
                                ptr(data.rotations), ptr(data.colors),
                                ptr(data.sphericalHarmonics), 3, 0) == 0
-    assert lib.gs3d_set_schedule(ctx, _lib.SCHEDULE_KEY_COUNT) == 0
+    from gs3d import learned
+    mp, mmean, mstd, mmetrics, mbound = learned.load(
+        ROOT / "webgpu-3dgs_gb300" / "gs3d" / "cost_mlp_c1.npz")
+    f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    mp, mmean, mstd = f32(mp), f32(mmean), f32(mstd)
+    assert lib.gs3d_set_cost_model(ctx, ptr(mp), ptr(mmean), ptr(mstd)) == 0
+    assert lib.gs3d_set_schedule(ctx, _lib.SCHEDULE_LEARNED if learned.gate(mmetrics, mbound)
+                                 else _lib.SCHEDULE_KEY_COUNT) == 0
     B = args.batch
     for step in range(args.profile):
         for b0 in range(0, len(cams), B):
