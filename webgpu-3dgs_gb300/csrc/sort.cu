@@ -41,7 +41,7 @@ constexpr int kItems = 8;
 constexpr uint32_t kPart = kPassThreads * kItems;  // 4096 keys per partition
 constexpr uint32_t kFlagAgg = 1u, kFlagInc = 2u;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
-constexpr int kLookback = 8;  // predecessor status words fetched per look-back step
+constexpr int kLookback = 16;  // predecessor status words fetched per look-back step
 
 template <typename K>
 struct KeyOps;
@@ -157,12 +157,32 @@ constexpr size_t part_buf_bytes() {
   return (size_t)kPart * (sizeof(K) + sizeof(uint32_t));
 }
 
-// One LSD pass.  Persistent CTAs claim 4096-key partitions in order and
-// double-buffer them: the partition after the current one is fetched by two
-// bulk (TMA) copies into the other shared-memory buffer while the current one
-// is ranked, reordered and written out.  Claiming one partition ahead cannot
-// deadlock: the smallest unfinished partition is always some CTA's current
-// one, and it waits only on smaller, finished partitions.
+// Inclusive scan over lanes 0..7 (the eight digit warps' totals).
+__device__ __forceinline__ uint32_t scan8_inclusive(uint32_t x, int lane) {
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+// One LSD pass.  Persistent CTAs claim 4096-key partitions in order.  A
+// partition is claimed when the CTA has resolved its current one (barrier C
+// below), and fetched by two bulk (TMA) copies into the other shared-memory
+// buffer while the current partition is written out; the claimed partition's
+// id travels with the buffer's mbarrier arrive.  Claiming late keeps the
+// window between a claim and the publication of the partition's digit counts
+// short, so successors' look-backs rarely find an unpublished predecessor.
+// Claiming cannot deadlock: the smallest unfinished partition is always some
+// CTA's current one, and it waits only on smaller, finished partitions.
+//
+// Three block barriers per partition:
+//   A  every warp has ranked its items (per-warp digit counts complete, the
+//      input buffer fully read into registers, the fetch landed everywhere);
+//   B  per-digit warp offsets and digit-warp prefix sums are in shared memory;
+//   C  the partition is reordered by digit and each digit's global
+//      destination is resolved.
 template <typename K, int NBITS>
 __global__ void __launch_bounds__(kPassThreads, 2)
     onesweep_kernel(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
@@ -172,11 +192,11 @@ __global__ void __launch_bounds__(kPassThreads, 2)
                     uint32_t* __restrict__ part_counter, uint32_t* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr size_t kBuf = part_buf_bytes<K>();
-  // [kWarps][256] per-warp digit counts, then exclusive offsets (<= 4096)
+  // [kWarps][256] per-warp digit counts, then per-warp exclusive offsets
   uint16_t* s_whist = reinterpret_cast<uint16_t*>(smem + 2 * kBuf);
-  __shared__ uint32_t s_bucket[kRadixBins], s_dstart[kRadixBins], s_dest[kRadixBins];
+  __shared__ uint32_t s_bucket[kRadixBins], s_dloc[kRadixBins], s_dest[kRadixBins];
   __shared__ uint32_t s_wsum[kWarps];
-  __shared__ uint32_t s_next;
+  __shared__ uint32_t s_part[2];  // partition id of each buffer
   __shared__ uint64_t s_bar[2];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -186,57 +206,52 @@ __global__ void __launch_bounds__(kPassThreads, 2)
   // the largest digit and ranks after every real item of it
   constexpr uint32_t kDigitMask = NBITS >= 8 ? 0xffu : ((1u << NBITS) - 1u);
 
-  auto issue = [&](uint32_t part, int b) {  // thread 0 only
-    unsigned char* buf = smem + b * kBuf;
-    const uint32_t kb = kPart * sizeof(K), vb = kPart * sizeof(uint32_t);
-    mbar_expect_tx(&s_bar[b], kb + vb);
-    bulk_g2s(buf, keys_in + (size_t)part * kPart, kb, &s_bar[b]);
-    bulk_g2s(buf + kb, vals_in + (size_t)part * kPart, vb, &s_bar[b]);
+  // one thread only: claim the next partition and start its fetch into buffer
+  // b (whose previous readers are past a block barrier), or, with no
+  // partition left, complete the buffer's phase empty
+  auto claim_into = [&](int b) {
+    const uint32_t part = atomicAdd(part_counter, 1u);
+    s_part[b] = part;  // published by the arrive below (release)
+    if (part < num_parts) {
+      unsigned char* buf = smem + b * kBuf;
+      const uint32_t kb = kPart * sizeof(K), vb = kPart * sizeof(uint32_t);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(&s_bar[b], kb + vb);
+      bulk_g2s(buf, keys_in + (size_t)part * kPart, kb, &s_bar[b]);
+      bulk_g2s(buf + kb, vals_in + (size_t)part * kPart, vb, &s_bar[b]);
+    } else {
+      mbar_arrive(&s_bar[b]);
+    }
   };
 
   const bool digit_thread = tid < kRadixBins;  // threads 0..255 own one digit each
-  // global bucket bases of this digit place
-  {
-    const uint32_t bb = block_exclusive_256(digit_thread ? __ldg(hist + tid) : 0u, s_wsum);
-    if (digit_thread) s_bucket[tid] = bb;
-  }
   if (tid == 0) {
     mbar_init(&s_bar[0], 1);
     mbar_init(&s_bar[1], 1);
     fence_mbar_init();
-    s_next = atomicAdd(part_counter, 1u);
-    if (s_next < num_parts) issue(s_next, 0);
+  }
+  // global bucket bases of this digit place (the scan's barriers also order
+  // the mbarrier initialisation before any wait)
+  {
+    const uint32_t bb = block_exclusive_256(digit_thread ? __ldg(hist + tid) : 0u, s_wsum);
+    if (digit_thread) s_bucket[tid] = bb;
   }
   __syncthreads();
-  uint32_t cur = s_next;
+  if (tid == 0) claim_into(0);
   int b = 0;
   uint32_t phase0 = 0, phase1 = 0;
 
-  while (cur < num_parts) {
-    // claim the next partition and fetch it into the other buffer, whose
-    // previous contents were fully written out before this barrier
-    __syncthreads();
-    if (tid == 0) {
-      const uint32_t nxt = atomicAdd(part_counter, 1u);
-      s_next = nxt;
-      if (nxt < num_parts) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        issue(nxt, b ^ 1);
-      }
-    }
-    for (int k = tid; k < kWarps * kRadixBins; k += kPassThreads) s_whist[k] = 0u;
+  for (;;) {
+    uint16_t* wh = s_whist + warp * kRadixBins;
+    // this warp's count row; its previous readers finished before barrier C
+    reinterpret_cast<uint4*>(wh)[lane] = make_uint4(0u, 0u, 0u, 0u);
+    __syncwarp();
     K* s_keys = reinterpret_cast<K*>(smem + b * kBuf);
     uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + b * kBuf + kPart * sizeof(K));
     const bool landed = mbar_wait(&s_bar[b], b ? phase1 : phase0);
     if (b) phase1 ^= 1u; else phase0 ^= 1u;
-    if (!__syncthreads_and(landed)) {  // bounded wait gave up: stop this CTA
-      if (tid == 0) latch_error(err, DEVERR_TIMEOUT);
-      break;
-    }
-    const uint32_t nxt = s_next;
-    const uint32_t part = cur;
-    const uint32_t base = part * kPart;
-    const uint32_t count = min(kPart, R - base);
+    const uint32_t part = landed ? s_part[b] : num_parts;
+    const uint32_t count = part < num_parts ? min(kPart, R - part * kPart) : 0u;
 
     // ---- registers <- shared (warp-striped: lane-contiguous) ----
     K key[kItems];
@@ -255,8 +270,6 @@ __global__ void __launch_bounds__(kPassThreads, 2)
       }
     }
     // ---- stable rank within the warp ----
-    uint16_t* wh = s_whist + warp * kRadixBins;
-    const uint32_t lt = lanemask_lt();
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const uint32_t d = KeyOps<K>::digit(key[i], word, shift) & kDigitMask;
@@ -265,9 +278,17 @@ __global__ void __launch_bounds__(kPassThreads, 2)
       __syncwarp();
       if ((__ffs(peers) - 1) == lane) wh[d] = (uint16_t)(prior + __popc(peers));
       __syncwarp();
-      dr[i] = d | ((prior + __popc(peers & lt)) << 8);
+      dr[i] = d | ((prior + __popc(peers & lanemask_lt())) << 8);
     }
-    __syncthreads();  // histograms complete; every item read out of the buffer
+    // A: counts complete, input buffer read, the fetch had landed for everyone
+    if (!__syncthreads_and(landed)) {  // bounded wait gave up: stop this CTA
+      if (tid == 0) {
+        latch_error(err, DEVERR_TIMEOUT);
+        mbar_wait(&s_bar[b], b ? phase1 ^ 1u : phase0 ^ 1u);  // one more bounded wait
+      }
+      break;
+    }
+    if (part >= num_parts) break;  // every thread read the same id
 
     // ---- per digit (thread = digit): warp offsets, partition totals ----
     uint32_t run = 0, pub = 0;
@@ -281,72 +302,83 @@ __global__ void __launch_bounds__(kPassThreads, 2)
       }
       pub = ((uint32_t)tid == kDigitMask) ? run - (kPart - count) : run;
       st_relaxed_u32(st, ((part == 0 ? kFlagInc : kFlagAgg) << 30) | pub);
+      const uint32_t inc = warp_inclusive(run, lane);
+      s_dloc[tid] = inc - run;  // exclusive within the digit warp
+      if (lane == 31) s_wsum[warp] = inc;
     }
-    const uint32_t dstart = block_exclusive_256(run, s_wsum);  // includes a barrier
-    if (digit_thread) s_dstart[tid] = dstart;
-    __syncthreads();
+    __syncthreads();  // B
+
+    // exclusive prefix of the eight digit warps' totals, lane w holds warp w's
+    const uint32_t wv = lane < 8 ? s_wsum[lane] : 0u;
+    const uint32_t wex = scan8_inclusive(wv, lane) - wv;
 
     // ---- reorder the partition in place ----
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
       const uint32_t d = dr[i] & 0xffu;
-      const uint32_t pos = s_dstart[d] + s_whist[warp * kRadixBins + d] + (dr[i] >> 8);
+      const uint32_t pos =
+          s_dloc[d] + __shfl_sync(0xffffffffu, wex, d >> 5) + wh[d] + (dr[i] >> 8);
       s_keys[pos] = key[i];
       s_vals[pos] = val[i];
     }
 
     // ---- decoupled look-back, one thread per digit ----
+    const uint32_t dstart = digit_thread ? s_dloc[tid] + __shfl_sync(0xffffffffu, wex, warp & 7)
+                                         : 0u;
     uint32_t excl = 0;
     bool ok = true;
     if (digit_thread && part > 0) {
-      // walk back a window of kLookback predecessors per step: their status
-      // words are fetched together, so one L2 round trip covers the window
+      // windows of kLookback predecessors: their status words are fetched
+      // together, so one L2 round trip covers the window
       int pp = (int)part - 1;
       bool found = false;
       while (!found && ok && pp >= 0) {
-        uint32_t w[kLookback];
+        uint32_t lw[kLookback];
 #pragma unroll
         for (int k = 0; k < kLookback; ++k)
-          w[k] = (pp - k >= 0) ? ld_relaxed_u32(status + (size_t)(pp - k) * kRadixBins + tid)
-                               : (kFlagInc << 30);
+          lw[k] = (pp - k >= 0) ? ld_relaxed_u32(status + (size_t)(pp - k) * kRadixBins + tid)
+                                : (kFlagInc << 30);
 #pragma unroll
         for (int k = 0; k < kLookback; ++k) {
           if (found || !ok) break;
           uint32_t spins = 0;
-          while ((w[k] >> 30) == 0u) {  // not published yet: poll this one
+          while ((lw[k] >> 30) == 0u) {  // not published yet: poll this one
             if (++spins > kSpinLimit) {
               ok = false;
               break;
             }
             if (spins > 16) __nanosleep(32);
-            w[k] = ld_relaxed_u32(status + (size_t)(pp - k) * kRadixBins + tid);
+            lw[k] = ld_relaxed_u32(status + (size_t)(pp - k) * kRadixBins + tid);
           }
           if (!ok) break;
-          excl += w[k] & kValueMask;
-          if ((w[k] >> 30) == kFlagInc) found = true;
+          excl += lw[k] & kValueMask;
+          if ((lw[k] >> 30) == kFlagInc) found = true;
         }
         pp -= kLookback;
       }
       st_relaxed_u32(st, (kFlagInc << 30) | ((excl + pub) & kValueMask));
     }
     if (digit_thread) s_dest[tid] = s_bucket[tid] + excl - dstart;
-    const int all_ok = __syncthreads_and(ok);
-    if (all_ok) {
-      // ---- write each digit run contiguously ----
-      for (uint32_t j = tid; j < count; j += kPassThreads) {
-        const K k = s_keys[j];
-        const uint32_t dst = s_dest[KeyOps<K>::digit(k, word, shift) & kDigitMask] + j;
-        if (dst < R) {
-          keys_out[dst] = k;
-          vals_out[dst] = s_vals[j];
-        } else {
-          latch_error(err, DEVERR_RANGE);
-        }
-      }
-    } else if (tid == 0) {
-      latch_error(err, DEVERR_TIMEOUT);  // nothing written for this partition
+    // C: partition reordered, destinations resolved
+    if (!__syncthreads_and(ok)) {  // nothing written for this partition
+      if (tid == 0) latch_error(err, DEVERR_TIMEOUT);
+      break;  // no fetch is in flight: the next claim comes after this barrier
     }
-    cur = nxt;
+    // the other buffer's last readers (previous write-out) passed barrier A;
+    // a thread without a digit claims, so the digit warps' write-out is not
+    // held up by the claim's round trip
+    if (tid == kRadixBins) claim_into(b ^ 1);
+    // ---- write each digit run contiguously ----
+    for (uint32_t j = tid; j < count; j += kPassThreads) {
+      const K k = s_keys[j];
+      const uint32_t dst = s_dest[KeyOps<K>::digit(k, word, shift) & kDigitMask] + j;
+      if (dst < R) {
+        keys_out[dst] = k;
+        vals_out[dst] = s_vals[j];
+      } else {
+        latch_error(err, DEVERR_RANGE);
+      }
+    }
     b ^= 1;
   }
 }
