@@ -245,6 +245,38 @@ int gs3d_get_view_info(struct gs3d_ctx* ctx, uint32_t view, gs3d_view_info* out)
  * under every schedule.  GS3D_SCHEDULE_LEARNED needs a cost model. */
 int gs3d_set_schedule(struct gs3d_ctx* ctx, uint32_t schedule);
 
+/* ---- tuning (extension) -----------------------------------------------------
+ * Knobs that change the speed of a rebin but never its image: for the same
+ * cameras every tuning renders bit-identical pixels (a pixel blends the
+ * splats whose radius circle covers it in (depth, splat id) order, whatever
+ * the tile grid), while the tile grid, key layout and tile_offsets follow
+ * tile_w x tile_h. */
+typedef struct gs3d_tuning {
+    uint32_t tile_w, tile_h;  /* tile pixel size (gs3d_set_tile_size)                 */
+    uint32_t digit_bits;      /* widest radix digit of the tile-id passes: 6 or 8     */
+    uint32_t raster_batch;    /* splats staged per raster batch: a multiple of 32 in
+                                 [32, 1024]; 0 = one per tile pixel                   */
+} gs3d_tuning;
+
+typedef struct gs3d_tune_result {
+    gs3d_tuning tuning;
+    float ms_per_view;        /* device time of one batched rebin / views             */
+    uint32_t tile_passes;     /* radix passes over the refs under this tuning         */
+    uint64_t refs;            /* live ref count of the measured batch                 */
+} gs3d_tune_result;
+
+int gs3d_set_tuning(struct gs3d_ctx* ctx, const gs3d_tuning* tuning);
+int gs3d_get_tuning(struct gs3d_ctx* ctx, gs3d_tuning* out);
+
+/* Autotuner: times the batched rebin of `views` (warm-up, then `reps` timed
+ * repetitions, CUDA events on the context's stream) under every candidate
+ * of tile size {8, 16, 32} square x digit width {6, 8} x raster batch
+ * {128, 256, 512}, applies the fastest and writes up to max_results
+ * measurements (n_results = candidates measured).  Blocking. */
+int gs3d_autotune(struct gs3d_ctx* ctx, const gs3d_view* views, uint32_t n_views,
+                  uint32_t reps, gs3d_tune_result* results, uint32_t max_results,
+                  uint32_t* n_results);
+
 /* Installs the cost MLP: GS3D_MLP_PARAMS f32 parameters and the per-feature
  * mean and standard deviation the features are normalized with (host
  * pointers). */

@@ -46,6 +46,9 @@ def test_null_arguments_are_rejected(built_lib):
     assert lib.gs3d_rebin(None, None, 1, 1) == _lib.ERR_INVALID_ARG
     assert lib.gs3d_synchronize(None) == _lib.ERR_INVALID_ARG
     assert lib.gs3d_prefix_scan_noalloc(None, None, 4, None) == _lib.ERR_INVALID_ARG
+    assert lib.gs3d_set_tuning(None, None) == _lib.ERR_INVALID_ARG
+    assert lib.gs3d_get_tuning(None, None) == _lib.ERR_INVALID_ARG
+    assert lib.gs3d_autotune(None, None, 0, 0, None, 0, None) == _lib.ERR_INVALID_ARG
     assert b"null" in lib.gs3d_last_error(None)
 
 

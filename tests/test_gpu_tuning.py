@@ -1,0 +1,102 @@
+"""Tuning knobs (tile size, tile-id digit width, raster batch depth) and the
+autotuner: every tuning renders the bit-identical image, and under any
+tuning the keys, values and tile ranges equal the oracle's for that tile
+grid."""
+import numpy as np
+import pytest
+
+from gs3d import GaussianSplatRenderer, Gs3dError, Scene, scenes
+from gs3d import _lib
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def renderer(built_lib):
+    r = GaussianSplatRenderer(Scene())
+    r.init()
+    yield r
+    r.destroy()
+
+
+def _views(n, sizes):
+    eyes = scenes.orbit_eyes(n, radius=10.0, jitter_deg=15.0, seed=3)
+    return [(0, scenes.camera_at(eyes[i], w, h).getUniformData(w, h), w, h)
+            for i, (w, h) in enumerate(sizes)]
+
+
+def _images(r, views):
+    return [r.readViewImage(v) for v in range(len(views))]
+
+
+def test_every_tuning_renders_the_same_image(renderer):
+    data = scenes.scene_clusters(150_000, seed=7, sh_degree=1)
+    renderer.setSplatData(data)
+    views = _views(3, [(640, 360), (1280, 720), (333, 217)])
+    renderer.setTuning(16, 8, 0)
+    renderer.rebinBatch(views)
+    want = _images(renderer, views)
+    for tile in (8, 16, 32):
+        for digit in (6, 8):
+            for batch in (0, 64, 512):
+                renderer.setTuning(tile, digit, batch)
+                renderer.rebinBatch(views)
+                got = _images(renderer, views)
+                for v in range(len(views)):
+                    assert np.array_equal(got[v].view(np.uint16), want[v].view(np.uint16)), \
+                        (tile, digit, batch, v)
+    renderer.setTuning(16, 8, 0)
+
+
+@pytest.mark.parametrize("tile,digit,batch", [(8, 6, 128), (32, 6, 512), (16, 6, 64)])
+def test_tuned_keys_match_the_oracle(renderer, oracle, tile, digit, batch):
+    """Single-view fused rebin under a non-default tuning: sorted keys,
+    values and tile_offsets bit-exact with the oracle's for that tile grid."""
+    data = scenes.scene_small(60_000, seed=11)
+    w, h = 1000, 563
+    u = scenes.small_camera(w, h).getUniformData(w, h)
+    o = oracle.rebin(u, w, h, tile, tile, data.positions, data.scales, data.rotations,
+                     data.colors, data.sphericalHarmonics, data.sphericalHarmonicsDegree)
+    renderer.setSplatData(data)
+    renderer.setTuning(tile, digit, batch)
+    renderer.rebin(data.splatCount, -(-w // tile), -(-h // tile), w, h, u)
+    R = renderer.refCount()
+    assert R == o["ref_counter"]
+    assert np.array_equal(renderer.readBuffer("sort_keys_a", R), o["sort_keys_a"])
+    assert np.array_equal(renderer.readBuffer("sort_values_a", R), o["sort_values_a"])
+    assert np.array_equal(renderer.readBuffer("tile_offsets"), o["tile_offsets"])
+    img = renderer.readImage().astype(np.float32)
+    assert np.abs(img - o["image"]).max() <= 2.0 / 255.0
+    renderer.setTuning(16, 8, 0)
+
+
+def test_autotune_applies_the_fastest_candidate(renderer):
+    data = scenes.scene_clusters(200_000, seed=2, sh_degree=0)
+    renderer.setSplatData(data)
+    views = _views(2, [(1280, 720), (960, 540)])
+    renderer.setTuning(16, 8, 0)
+    renderer.rebinBatch(views)
+    want = _images(renderer, views)
+    res = renderer.autotune(views, reps=2)
+    assert len(res) == 3 * 2 * 3
+    assert all(r["ms_per_view"] > 0 for r in res)
+    best = renderer.getTuning()
+    assert (best["tile"], best["digit_bits"], best["raster_batch"]) == \
+        (res[0]["tile"], res[0]["digit_bits"], res[0]["raster_batch"])
+    # fewer refs with larger tiles; the 6-bit digit never needs fewer passes
+    by = {(r["tile"][0], r["digit_bits"], r["raster_batch"]): r for r in res}
+    assert by[(32, 8, 256)]["refs"] < by[(16, 8, 256)]["refs"] < by[(8, 8, 256)]["refs"]
+    assert by[(16, 6, 256)]["tile_passes"] >= by[(16, 8, 256)]["tile_passes"]
+    renderer.rebinBatch(views)
+    got = _images(renderer, views)
+    for v in range(len(views)):
+        assert np.array_equal(got[v].view(np.uint16), want[v].view(np.uint16))
+    renderer.setTuning(16, 8, 0)
+
+
+def test_bad_tunings_are_rejected(renderer):
+    for bad in [(16, 7, 0), (16, 8, 48), (16, 8, 2048), (64, 8, 0)]:
+        with pytest.raises(Gs3dError) as ei:
+            renderer.setTuning(*bad)
+        assert ei.value.code == _lib.ERR_INVALID_ARG
+    renderer.setTuning(16, 8, 0)

@@ -63,6 +63,8 @@ struct gs3d_ctx {
   std::string err = "no error";
 
   uint32_t tile_w = 16, tile_h = 16, max_tiles_per_splat = 16;
+  uint32_t digit_bits = 8;    // widest tile-id radix digit (gs3d_tuning)
+  uint32_t raster_batch = 0;  // splats per raster batch, 0 = tile area (gs3d_tuning)
   uint32_t flags = 0;
   uint32_t schedule = GS3D_SCHEDULE_ROW_MAJOR;
 
@@ -457,8 +459,8 @@ int require_single(gs3d_ctx* c, const char* stage) {
   return GS3D_OK;
 }
 
-SortPlan tile_digit_plan(uint32_t num_tiles) {
-  const SortPlan full = make_sort_plan(num_tiles);
+SortPlan tile_digit_plan(uint32_t num_tiles, uint32_t digit_bits) {
+  const SortPlan full = make_sort_plan(num_tiles, (int)digit_bits);
   SortPlan tp{};
   for (int p = 4; p < full.passes; ++p) {  // the tile-id digit places only
     tp.word[tp.passes] = full.word[p];
@@ -510,6 +512,7 @@ int raster_stage(gs3d_ctx* c, bool culled) {
   a.tile_costs = u32(c->tile_costs);
   a.order = order;
   a.queue_counter = &ctrl_of(c)->raster_queue;
+  a.batch = c->raster_batch;
   a.culled = culled;
   CK(cudaMemsetAsync(a.queue_counter, 0, sizeof(uint32_t), c->stream), "reset raster queue");
   CK(launch_raster(a, c->sm_count, c->stream), "rasterize_tiles");
@@ -551,7 +554,7 @@ int fused_rebin(gs3d_ctx* c) {
                    c->scan_epoch, u32(c->ref_counter), &k->error, c->stream),
        "prefix scan (depth order)");
   }
-  const SortPlan tp = tile_digit_plan(c->total_tiles);
+  const SortPlan tp = tile_digit_plan(c->total_tiles, c->digit_bits);
   {
     StageScope t(c, GS3D_STAGE_EMIT);
     CK(launch_emit_sorted(dviews(c), nv, c->total_splats,
@@ -590,8 +593,9 @@ void destroy_graph(gs3d_ctx* c) {
 }
 
 std::vector<uint64_t> graph_signature(gs3d_ctx* c) {
-  std::vector<uint64_t> sig = {c->views.size(), c->tile_w, c->tile_h, c->schedule,
-                               c->capacity, c->alloc_gen, c->max_sh,
+  std::vector<uint64_t> sig = {c->views.size(), c->tile_w,     c->tile_h,
+                               c->schedule,     c->capacity,   c->alloc_gen,
+                               c->max_sh,       c->digit_bits, c->raster_batch,
                                c->flags & ~GS3D_FLAG_STAGE_TIMING};
   for (const ViewDesc& v : c->views) {
     sig.push_back((uint64_t)(uintptr_t)v.pos);
@@ -877,7 +881,7 @@ int gs3d_radix_sort(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
   TRY(require_single(c, "radix_sort"));
   TRY(set_device(c));
-  const SortPlan plan = make_sort_plan(c->total_tiles);
+  const SortPlan plan = make_sort_plan(c->total_tiles, (int)c->digit_bits);
   {
     StageScope t(c, GS3D_STAGE_SORT);
     CK(launch_sort(plan, u32(c->ref_counter), c->capacity, static_cast<uint2*>(c->keys_a.p),
@@ -953,6 +957,108 @@ int gs3d_get_view_info(gs3d_ctx* c, uint32_t view, gs3d_view_info* out) {
     return fail(c, GS3D_ERR_INVALID_ARG, "view %u out of range (%zu views)", view,
                 c->info.size());
   *out = c->info[view];
+  return GS3D_OK;
+}
+
+int gs3d_set_tuning(gs3d_ctx* c, const gs3d_tuning* t) {
+  if (!c || !t) return fail(c, GS3D_ERR_INVALID_ARG, "null tuning");
+  if (t->digit_bits != 6 && t->digit_bits != 8)
+    return fail(c, GS3D_ERR_INVALID_ARG, "digit_bits must be 6 or 8 (got %u)", t->digit_bits);
+  if (t->raster_batch % 32 != 0 || t->raster_batch > 1024)
+    return fail(c, GS3D_ERR_INVALID_ARG,
+                "raster_batch must be 0 or a multiple of 32 up to 1024 (got %u)",
+                t->raster_batch);
+  if (t->tile_w == 0 || t->tile_h == 0 || t->tile_w * t->tile_h > 1024)
+    return fail(c, GS3D_ERR_INVALID_ARG, "tile %ux%u: 1..1024 pixels", t->tile_w, t->tile_h);
+  TRY(gs3d_set_tile_size(c, t->tile_w, t->tile_h, nullptr, nullptr));
+  c->digit_bits = t->digit_bits;
+  c->raster_batch = t->raster_batch;
+  return GS3D_OK;
+}
+
+int gs3d_get_tuning(gs3d_ctx* c, gs3d_tuning* out) {
+  if (!c || !out) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
+  out->tile_w = c->tile_w;
+  out->tile_h = c->tile_h;
+  out->digit_bits = c->digit_bits;
+  out->raster_batch = c->raster_batch;
+  return GS3D_OK;
+}
+
+int gs3d_autotune(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views, uint32_t reps,
+                  gs3d_tune_result* results, uint32_t max_results, uint32_t* n_results) {
+  if (!c || !views || n_views == 0)
+    return fail(c, GS3D_ERR_INVALID_ARG, "autotune needs at least one view");
+  if (!c->have_scene) return fail(c, GS3D_ERR_STATE, "autotune: no scene");
+  TRY(set_device(c));
+  if (n_results) *n_results = 0;
+  if (reps == 0) reps = 3;
+  gs3d_tuning saved{};
+  TRY(gs3d_get_tuning(c, &saved));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0), "autotune event");
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fail(c, GS3D_ERR_CUDA, "autotune event");
+  }
+  std::vector<gs3d_tune_result> res;
+  int rc = GS3D_OK;
+  const uint32_t tiles[] = {8, 16, 32}, digits[] = {6, 8}, batches[] = {128, 256, 512};
+  for (uint32_t tile : tiles) {
+    for (uint32_t digit : digits) {
+      for (uint32_t batch : batches) {
+        const gs3d_tuning t{tile, tile, digit, batch};
+        rc = gs3d_set_tuning(c, &t);
+        if (rc != GS3D_OK) break;
+        // warm-up: sizes the key buffers (capacity retries), captures the graph
+        int wr = GS3D_ERR_CAPACITY;
+        for (int attempt = 0; attempt < 3 && wr == GS3D_ERR_CAPACITY; ++attempt) {
+          wr = gs3d_rebin_batch(c, views, n_views);
+          if (wr == GS3D_OK) wr = gs3d_synchronize(c);
+        }
+        if (wr == GS3D_ERR_CAPACITY) continue;  // beyond the ref limit under this tile size
+        if (wr != GS3D_OK) {
+          rc = wr;
+          break;
+        }
+        cudaEventRecord(e0, c->stream);
+        for (uint32_t r = 0; r < reps && rc == GS3D_OK; ++r) rc = gs3d_rebin_batch(c, views, n_views);
+        cudaEventRecord(e1, c->stream);
+        if (rc == GS3D_OK) rc = gs3d_synchronize(c);
+        if (rc != GS3D_OK) break;
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+          rc = fail(c, GS3D_ERR_CUDA, "autotune timing");
+          break;
+        }
+        uint32_t refs = 0;
+        rc = gs3d_ref_count(c, &refs);
+        if (rc != GS3D_OK) break;
+        gs3d_tune_result r{};
+        r.tuning = t;
+        r.ms_per_view = ms / (float)reps / (float)n_views;
+        r.tile_passes = (uint32_t)tile_digit_plan(c->total_tiles, digit).passes;
+        r.refs = refs;
+        res.push_back(r);
+      }
+      if (rc != GS3D_OK) break;
+    }
+    if (rc != GS3D_OK) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != GS3D_OK || res.empty()) {
+    const std::string why = rc != GS3D_OK ? c->err : std::string("no candidate fitted");
+    gs3d_set_tuning(c, &saved);
+    return fail(c, rc != GS3D_OK ? rc : GS3D_ERR_CAPACITY, "autotune: %s", why.c_str());
+  }
+  size_t best = 0;
+  for (size_t i = 1; i < res.size(); ++i)
+    if (res[i].ms_per_view < res[best].ms_per_view) best = i;
+  TRY(gs3d_set_tuning(c, &res[best].tuning));
+  if (results)
+    for (size_t i = 0; i < res.size() && i < max_results; ++i) results[i] = res[i];
+  if (n_results) *n_results = (uint32_t)res.size();
   return GS3D_OK;
 }
 

@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kThreads)
                        const uint32_t* __restrict__ sorted_offsets,
                        const uint32_t* __restrict__ ref_counter, uint32_t capacity,
                        uint2* __restrict__ keys, uint32_t* __restrict__ values, int4 shifts,
-                       uint32_t* __restrict__ g_hist, uint32_t* __restrict__ err) {
+                       uint4 masks, uint32_t* __restrict__ g_hist, uint32_t* __restrict__ err) {
   __shared__ uint32_t s_off[kThreads + 1];
   __shared__ uint32_t s_tminx[kThreads], s_tminy[kThreads], s_w[kThreads], s_cnt[kThreads];
   __shared__ uint32_t s_lo[kThreads], s_id[kThreads], s_tx[kThreads], s_tb[kThreads];
@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(kThreads)
     return;
   }
   const int sh[4] = {shifts.x, shifts.y, shifts.z, shifts.w};
+  const uint32_t mk[4] = {masks.x, masks.y, masks.z, masks.w};
   for (uint32_t base = begin; base < end; base += kThreads) {  // warp-uniform trip count
     const uint32_t j = base + threadIdx.x;
     bool live = j < end;
@@ -164,7 +165,7 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
 #pragma unroll
-    for (int p = 0; p < TP; ++p) hist_add_256(s_hist[p], (tile >> sh[p]) & 0xffu, live);
+    for (int p = 0; p < TP; ++p) hist_add_256(s_hist[p], (tile >> sh[p]) & mk[p], live);
   }
   __syncthreads();
   for (int k = threadIdx.x; k < TP * kRadixBins; k += kThreads) {
@@ -184,13 +185,18 @@ cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t
   if (n == 0) return cudaSuccess;
   const uint32_t blocks = (n + kThreads - 1) / kThreads;
   int4 sh = make_int4(0, 0, 0, 0);
+  uint4 mk = make_uint4(0, 0, 0, 0);
   int* shp = &sh.x;
-  for (int p = 0; p < tile_plan.passes && p < 4; ++p) shp[p] = tile_plan.shift[p];
+  uint32_t* mkp = &mk.x;
+  for (int p = 0; p < tile_plan.passes && p < 4; ++p) {
+    shp[p] = tile_plan.shift[p];
+    mkp[p] = digit_mask(tile_plan.nbits[p]);
+  }
 #define GS3D_EMIT_CASE(TP)                                                                     \
   case TP:                                                                                    \
     emit_sorted_kernel<TP><<<blocks, kThreads, 0, s>>>(views, n_views, n, proj, sorted_ids,    \
                                                        sorted_offsets, ref_counter, capacity,  \
-                                                       keys, values, sh, g_hist, err);         \
+                                                       keys, values, sh, mk, g_hist, err);     \
     break;
   switch (tile_plan.passes) {
     GS3D_EMIT_CASE(0)

@@ -198,9 +198,14 @@ struct SortPlan {
   int passes;                    // number of digit passes (digits of up to 8 bits)
   int word[kMaxSortPasses];      // 0 = hi (tile id), 1 = lo (depth bits)
   int shift[kMaxSortPasses];
-  int nbits[kMaxSortPasses];     // significant bits of the digit (0 = 8)
+  int nbits[kMaxSortPasses];     // digit width of the pass: 2, 4, 6 or 8
 };
-SortPlan make_sort_plan(uint32_t num_tiles);
+// 4 depth-bit passes, then the tile-id bits below the highest set bit of
+// num_tiles - 1 in digits of at most tile_digit_bits (6 or 8) bits.  A digit
+// is (word >> shift) & ((1 << nbits) - 1); digits of neighbouring passes may
+// overlap by a bit, which a stable LSD sequence tolerates.
+SortPlan make_sort_plan(uint32_t num_tiles, int tile_digit_bits = 8);
+__host__ __device__ inline uint32_t digit_mask(int nbits) { return (1u << nbits) - 1u; }
 
 // Projects every splat-view of the batch (total_blocks = sum of
 // ceil(splat_count / 256) over views; max_sh_degree bounds the views' SH
@@ -303,6 +308,7 @@ struct RasterArgs {
   uint32_t* tile_costs;   // may be null
   const uint32_t* order;  // may be null
   uint32_t* queue_counter;
+  uint32_t batch;         // splats staged per batch (0 = tile_w * tile_h)
   bool culled;
 };
 cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s);

@@ -9,9 +9,10 @@
 // the output is rgba16float (C, 1 - T), premultiplied, no background.
 //
 // GB300 specifics:
-//  * each batch of sorted splats is staged into shared memory with 16-byte
-//    cp.async copies, double-buffered so the next batch streams in while the
-//    current one is blended;
+//  * each batch of sorted splats (RasterArgs::batch splats, by default one
+//    per tile pixel) is staged into shared memory with 16-byte cp.async
+//    copies, double-buffered so the next batch streams in while the current
+//    one is blended;
 //  * the CTA leaves as soon as a block-wide vote finds every pixel
 //    terminated (the reference keeps looping over the remaining batches);
 //  * each staged splat is converted once per tile into pre-scaled conic
@@ -34,6 +35,8 @@
 // math differs only in rounding (log2-domain exponent, fused multiply-adds),
 // which the 2/255 image tolerance covers.
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 #include "gs3d_internal.cuh"
 
@@ -110,15 +113,20 @@ __device__ __forceinline__ void store_pixel(uint2* image, uint32_t W, uint32_t p
       make_uint2(*reinterpret_cast<const uint32_t*>(&rg), *reinterpret_cast<const uint32_t*>(&ba));
 }
 
+// Stages sorted splats [first, min(first + batch, end)) into dst; thread t
+// copies entries t, t + nt, ... (one commit group per thread and batch).
 __device__ __forceinline__ void stage_batch(const gs3d_projected_splat* __restrict__ proj,
-                                            const uint32_t* __restrict__ values, uint32_t idx,
-                                            uint32_t end, SplatStage* dst) {
-  if (idx < end) {
+                                            const uint32_t* __restrict__ values, uint32_t first,
+                                            uint32_t end, uint32_t batch, uint32_t nt,
+                                            SplatStage* dst) {
+  for (uint32_t k = threadIdx.x; k < batch; k += nt) {
+    const uint32_t idx = first + k;
+    if (idx >= end) break;
     const uint32_t id = __ldg(values + idx);
     const float4* src = reinterpret_cast<const float4*>(proj + id);
-    cp_async16(&dst->a, src + 0);
-    cp_async16(&dst->b, src + 1);
-    cp_async16(&dst->c, src + 2);
+    cp_async16(&dst[k].a, src + 0);
+    cp_async16(&dst[k].b, src + 1);
+    cp_async16(&dst[k].c, src + 2);
   }
   cp_async_commit();
 }
@@ -174,7 +182,8 @@ __device__ __forceinline__ TileGeom tile_geom(const RasterArgs& a, uint32_t t) {
 // One thread per pixel, linear pixel order (the reference's layout).
 __device__ void raster_tile_plain(const RasterArgs& a, const TileGeom& g, SplatStage* buf0,
                                   SplatStage* buf1, uint32_t* s_cost) {
-  const uint32_t nt = a.tile_w * a.tile_h;  // == blockDim.x == batch size
+  const uint32_t nt = a.tile_w * a.tile_h;  // == blockDim.x
+  const uint32_t D = a.batch ? a.batch : nt;  // splats per staged batch
   const uint32_t tid = threadIdx.x;
   const uint32_t px = g.ox + tid % a.tile_w;
   const uint32_t py = g.oy + tid / a.tile_w;
@@ -184,34 +193,33 @@ __device__ void raster_tile_plain(const RasterArgs& a, const TileGeom& g, SplatS
   const uint32_t start = __ldg(a.tile_offsets + g.tile);
   const uint32_t end = __ldg(a.tile_offsets + g.tile + 1);
   const uint32_t len = end > start ? end - start : 0u;
-  const uint32_t nbatches = (len + nt - 1) / nt;
+  const uint32_t nbatches = (len + D - 1) / D;
 
   Pixel p{0.f, 0.f, 0.f, 1.0f};
   bool done = !in_bounds;
   uint32_t used = 0;
 
-  if (nbatches > 0) stage_batch(a.proj, a.values, start + tid, end, buf0 + tid);
+  if (nbatches > 0) stage_batch(a.proj, a.values, start, end, D, nt, buf0);
   for (uint32_t bi = 0; bi < nbatches; ++bi) {
     SplatStage* cur = (bi & 1) ? buf1 : buf0;
     if (bi + 1 < nbatches) {
-      stage_batch(a.proj, a.values, start + (bi + 1) * nt + tid, end,
-                  ((bi & 1) ? buf0 : buf1) + tid);
+      stage_batch(a.proj, a.values, start + (bi + 1) * D, end, D, nt, (bi & 1) ? buf0 : buf1);
       cp_async_wait<1>();
     } else {
       cp_async_wait<0>();
     }
-    const uint32_t cnt = min(nt, end - (start + bi * nt));
-    if (tid < cnt) prepare(cur[tid]);  // own copy is complete
+    const uint32_t cnt = min(D, end - (start + bi * D));
+    for (uint32_t k = tid; k < cnt; k += nt) prepare(cur[k]);  // own copies are complete
     __syncthreads();
     if (!done) {
       for (uint32_t j = 0; j < cnt; ++j) {
         if (blend_one<true>(pfx, pfy, cur[j], p, true)) {
           done = true;
-          used = bi * nt + j + 1;
+          used = bi * D + j + 1;
           break;
         }
       }
-      if (!done) used = bi * nt + cnt;
+      if (!done) used = bi * D + cnt;
     }
     if (__syncthreads_and(done)) {
       cp_async_wait<0>();  // drain the prefetch of the next batch before leaving
@@ -230,6 +238,7 @@ __device__ void raster_tile_plain(const RasterArgs& a, const TileGeom& g, SplatS
 __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, SplatStage* buf0,
                                    SplatStage* buf1, uint32_t* s_cost) {
   const uint32_t nt = a.tile_w * a.tile_h;
+  const uint32_t D = a.batch ? a.batch : nt;  // splats per staged batch
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   uint32_t lx, ly;
   if ((a.tile_w % 8 == 0) && (a.tile_h % 4 == 0)) {  // 8x4 pixel block per warp
@@ -257,24 +266,23 @@ __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, Splat
   const uint32_t start = __ldg(a.tile_offsets + g.tile);
   const uint32_t end = __ldg(a.tile_offsets + g.tile + 1);
   const uint32_t len = end > start ? end - start : 0u;
-  const uint32_t nbatches = (len + nt - 1) / nt;
+  const uint32_t nbatches = (len + D - 1) / D;
 
   Pixel p{0.f, 0.f, 0.f, 1.0f};
   bool done = !in_bounds;
   uint32_t used = 0;
 
-  if (nbatches > 0) stage_batch(a.proj, a.values, start + tid, end, buf0 + tid);
+  if (nbatches > 0) stage_batch(a.proj, a.values, start, end, D, nt, buf0);
   for (uint32_t bi = 0; bi < nbatches; ++bi) {
     SplatStage* cur = (bi & 1) ? buf1 : buf0;
     if (bi + 1 < nbatches) {
-      stage_batch(a.proj, a.values, start + (bi + 1) * nt + tid, end,
-                  ((bi & 1) ? buf0 : buf1) + tid);
+      stage_batch(a.proj, a.values, start + (bi + 1) * D, end, D, nt, (bi & 1) ? buf0 : buf1);
       cp_async_wait<1>();
     } else {
       cp_async_wait<0>();
     }
-    const uint32_t cnt = min(nt, end - (start + bi * nt));
-    if (tid < cnt) prepare(cur[tid]);  // own copy is complete
+    const uint32_t cnt = min(D, end - (start + bi * D));
+    for (uint32_t k = tid; k < cnt; k += nt) prepare(cur[k]);  // own copies are complete
     __syncthreads();
     if (__any_sync(0xffffffffu, !done)) {
       for (uint32_t k0 = 0; k0 < cnt; k0 += 32) {
@@ -286,12 +294,12 @@ __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, Splat
           mask &= mask - 1;
           if (blend_one<false>(pfx, pfy, cur[k0 + b], p, !done)) {
             done = true;
-            used = bi * nt + k0 + b + 1;
+            used = bi * D + k0 + b + 1;
           }
         }
         if (__all_sync(0xffffffffu, done)) break;
       }
-      if (!done) used = bi * nt + cnt;
+      if (!done) used = bi * D + cnt;
     }
     if (__syncthreads_and(done)) {
       cp_async_wait<0>();
@@ -308,9 +316,9 @@ __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, Splat
 template <bool CULLED>
 __global__ void raster_kernel(RasterArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const uint32_t nt = a.tile_w * a.tile_h;
+  const uint32_t D = a.batch ? a.batch : a.tile_w * a.tile_h;
   SplatStage* buf0 = reinterpret_cast<SplatStage*>(smem);
-  SplatStage* buf1 = buf0 + nt;
+  SplatStage* buf1 = buf0 + D;
   __shared__ uint32_t s_item, s_cost;
   while (true) {
     if (threadIdx.x == 0) {
@@ -336,20 +344,33 @@ __global__ void raster_kernel(RasterArgs a) {
 cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s) {
   if (a.num_tiles == 0) return cudaSuccess;
   const uint32_t nt = a.tile_w * a.tile_h;
+  if (a.batch % 32 != 0 || a.batch > 1024) return cudaErrorInvalidValue;
+  const uint32_t D = a.batch ? a.batch : nt;
   const bool culled = a.culled && (nt % 32 == 0);
-  const size_t smem = 2 * (size_t)nt * sizeof(SplatStage);
+  const size_t smem = 2 * (size_t)D * sizeof(SplatStage);
   auto kern = culled ? raster_kernel<true> : raster_kernel<false>;
-  // launch configuration per (variant, tile area), computed once per process
-  static int cache[2][1025] = {};
-  int& per_sm = cache[culled ? 1 : 0][nt];
+  // launch configuration per (variant, tile area, batch), computed once per process
+  static std::mutex mu;
+  static std::map<uint64_t, int> cache;
+  const uint64_t key = ((uint64_t)(culled ? 1 : 0) << 40) | ((uint64_t)nt << 20) | D;
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) per_sm = it->second;
+  }
   if (per_sm == 0) {
+    // one attribute per kernel, set to the largest batch's footprint so that
+    // configurations cached earlier keep fitting
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)std::max<size_t>(smem, 48 * 1024));
+                                         (int)(2 * 1024 * sizeof(SplatStage)));
     if (e != cudaSuccess) return e;
     int n = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, (int)nt, smem);
     if (e != cudaSuccess) return e;
     per_sm = std::max(n, 1);
+    std::lock_guard<std::mutex> lock(mu);
+    cache[key] = per_sm;
   }
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
       a.num_tiles, (uint64_t)sm_count * (uint64_t)std::max(per_sm, 1));

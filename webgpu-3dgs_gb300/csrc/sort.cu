@@ -108,6 +108,7 @@ __device__ __forceinline__ uint32_t match_digit(uint32_t d) {
 struct PassDev {
   int word[kMaxSortPasses];
   int shift[kMaxSortPasses];
+  uint32_t mask[kMaxSortPasses];
 };
 
 // Histogram of every sorted digit place + clear of the look-back status.
@@ -133,17 +134,20 @@ __global__ void __launch_bounds__(kThreads)
   }
 
   int word[P], shift[P];
+  uint32_t mask[P];
 #pragma unroll
   for (int p = 0; p < P; ++p) {
     word[p] = pd.word[p];
     shift[p] = pd.shift[p];
+    mask[p] = pd.mask[p];
   }
   for (size_t base = (size_t)blockIdx.x * kThreads; base < R; base += gstride) {
     const size_t idx = base + threadIdx.x;
     const bool in = idx < R;
     const K k = in ? keys[idx] : KeyOps<K>::sentinel();
 #pragma unroll
-    for (int p = 0; p < P; ++p) hist_add_256(s_hist[p], KeyOps<K>::digit(k, word[p], shift[p]), in);
+    for (int p = 0; p < P; ++p)
+      hist_add_256(s_hist[p], KeyOps<K>::digit(k, word[p], shift[p]) & mask[p], in);
   }
   __syncthreads();
   for (int k = threadIdx.x; k < P * kRadixBins; k += kThreads) {
@@ -418,7 +422,7 @@ cudaError_t launch_pass(int nbits, const K* kin, const uint32_t* vin, K* kout, u
                                                               shift, hist, status,           \
                                                               part_counter, err);            \
   break;
-  switch (nbits <= 2 ? 2 : nbits <= 4 ? 4 : nbits <= 6 ? 6 : 8) {
+  switch (nbits) {  // 2, 4, 6 or 8 (make_sort_plan)
     case 2: GS3D_PASS(2)
     case 4: GS3D_PASS(4)
     case 6: GS3D_PASS(6)
@@ -468,6 +472,7 @@ cudaError_t run_passes(const SortPlan& plan, const uint32_t* ref_counter, uint32
   for (int p = 0; p < plan.passes; ++p) {
     pd.word[p] = plan.word[p];
     pd.shift[p] = plan.shift[p];
+    pd.mask[p] = digit_mask(plan.nbits[p]);
   }
   if (!hist_ready) {
     e = launch_histogram<K>(plan.passes, pd, keys_a, ref_counter, capacity, g_hist, status,
@@ -478,8 +483,7 @@ cudaError_t run_passes(const SortPlan& plan, const uint32_t* ref_counter, uint32
   if (e != cudaSuccess) return e;
   for (int p = 0; p < plan.passes; ++p) {
     const bool even = (p % 2) == 0;
-    const int nbits = plan.nbits[p] > 0 ? plan.nbits[p] : 8;
-    e = launch_pass<K>(nbits, even ? keys_a : keys_b, even ? vals_a : vals_b,
+    e = launch_pass<K>(plan.nbits[p], even ? keys_a : keys_b, even ? vals_a : vals_b,
                        even ? keys_b : keys_a, even ? vals_b : vals_a, ref_counter, capacity,
                        plan.word[p], plan.shift[p], g_hist + (size_t)p * kRadixBins,
                        status + (size_t)p * stride, part_counters + p, err, sm_count, parts_cap,
@@ -491,7 +495,7 @@ cudaError_t run_passes(const SortPlan& plan, const uint32_t* ref_counter, uint32
 
 }  // namespace
 
-SortPlan make_sort_plan(uint32_t num_tiles) {
+SortPlan make_sort_plan(uint32_t num_tiles, int tile_digit_bits) {
   SortPlan p{};
   int n = 0;
   for (int s = 0; s < 32; s += 8) {  // depth bits (lo word)
@@ -502,10 +506,15 @@ SortPlan make_sort_plan(uint32_t num_tiles) {
   }
   const uint32_t max_tile = num_tiles > 0 ? num_tiles - 1 : 0;
   const int bits = max_tile ? 32 - __builtin_clz(max_tile) : 0;
-  for (int s = 0; s < bits; s += 8) {  // tile-id bits (hi word)
+  // at most kMaxSortPasses - 4 tile passes: wider digits when narrow ones
+  // would need more
+  int w = tile_digit_bits == 6 ? 6 : 8;
+  if ((bits + w - 1) / w > kMaxSortPasses - 4) w = 8;
+  for (int s = 0; s < bits; s += w) {  // tile-id bits (hi word)
+    const int left = bits - s < w ? bits - s : w;  // the top digit may be narrower
     p.word[n] = 0;
     p.shift[n] = s;
-    p.nbits[n] = bits - s < 8 ? bits - s : 8;  // the top digit may be narrower
+    p.nbits[n] = (left + 1) & ~1;  // kernels exist for 2, 4, 6 and 8 bits
     ++n;
   }
   p.passes = n;

@@ -66,6 +66,16 @@ class View_t(C.Structure):
                 ("height", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class Tuning_t(C.Structure):
+    _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("digit_bits", C.c_uint32),
+                ("raster_batch", C.c_uint32)]
+
+
+class TuneResult_t(C.Structure):
+    _fields_ = [("tuning", Tuning_t), ("ms_per_view", C.c_float), ("tile_passes", C.c_uint32),
+                ("refs", C.c_uint64)]
+
+
 class ViewInfo_t(C.Structure):
     _fields_ = [("pixel_offset", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32),
                 ("tiles_x", C.c_uint32), ("tiles_y", C.c_uint32), ("tile_base", C.c_uint32),
@@ -92,6 +102,9 @@ SIGNATURES = {
     "gs3d_rebin_batch": ([_P, _P, _U32], _I),
     "gs3d_get_view_info": ([_P, _U32, C.POINTER(ViewInfo_t)], _I),
     "gs3d_set_schedule": ([_P, _U32], _I),
+    "gs3d_set_tuning": ([_P, C.POINTER(Tuning_t)], _I),
+    "gs3d_get_tuning": ([_P, C.POINTER(Tuning_t)], _I),
+    "gs3d_autotune": ([_P, _P, _U32, _U32, C.POINTER(TuneResult_t), _U32, C.POINTER(_U32)], _I),
     "gs3d_set_tile_size": ([_P, _U32, _U32, C.POINTER(_U32), C.POINTER(_U32)], _I),
     "gs3d_set_camera": ([_P, C.POINTER(Camera_t), _U32, _U32], _I),
     "gs3d_preprocess": ([_P], _I),

@@ -170,6 +170,47 @@ class GaussianSplatRenderer:
         self.setSchedule(_lib.SCHEDULE_LEARNED)
         return True
 
+    def setTuning(self, tile: int | tuple[int, int] = 16, digit_bits: int = 8,
+                  raster_batch: int = 0) -> None:
+        """Speed knobs that leave every image bit-identical: square (or
+        (w, h)) tile size, widest tile-id radix digit (6 or 8 bits), splats
+        staged per raster batch (0 = one per tile pixel)."""
+        tw, th = (tile, tile) if isinstance(tile, int) else tile
+        t = _lib.Tuning_t(int(tw), int(th), int(digit_bits), int(raster_batch))
+        self._call("gs3d_set_tuning", C.byref(t))
+        self.setTileSize(tw, th)
+
+    def getTuning(self) -> dict:
+        t = _lib.Tuning_t()
+        self._call("gs3d_get_tuning", C.byref(t))
+        return {"tile": (t.tile_w, t.tile_h), "digit_bits": t.digit_bits,
+                "raster_batch": t.raster_batch}
+
+    def autotune(self, views, reps: int = 3) -> list[dict]:
+        """Times the batched rebin of views ((scene, camera_uniform, w, h)
+        tuples) under every candidate tuning, applies the fastest and returns
+        the measurements, fastest first."""
+        views = list(views)
+        arr = (_lib.View_t * len(views))()
+        for i, (scene, u, w, h) in enumerate(views):
+            arr[i].camera = camera_struct(u)
+            arr[i].scene = int(scene)
+            arr[i].width = int(w)
+            arr[i].height = int(h)
+        out = (_lib.TuneResult_t * 64)()
+        n = C.c_uint32()
+        self._call("gs3d_autotune", C.cast(arr, C.c_void_p), len(views), int(reps), out, 64,
+                   C.byref(n))
+        best = self.getTuning()
+        self.tileSizeX, self.tileSizeY = best["tile"]
+        self.scene.tiles = list(best["tile"])
+        self.lastViewport = (-1, -1)
+        res = [{"tile": (r.tuning.tile_w, r.tuning.tile_h), "digit_bits": r.tuning.digit_bits,
+                "raster_batch": r.tuning.raster_batch, "ms_per_view": float(r.ms_per_view),
+                "tile_passes": int(r.tile_passes), "refs": int(r.refs)}
+               for r in out[:n.value]]
+        return sorted(res, key=lambda r: r["ms_per_view"])
+
     def setAlwaysRebin(self, on: bool) -> None:
         self.alwaysRebin = bool(on)
 
