@@ -35,8 +35,9 @@ sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "webgpu-3dgs_gb300"))
 
 METRIC = "views/s at 3M Gaussians 1080p, learned+batched vs plain, same image"
-WORKLOAD = ("3M Gaussians fp32 SH3 (64 clusters, seed 0), 1920x1080, 16x16 tiles, "
-            "64-pose orbit r=12 +-20deg")
+WORKLOAD = ("3M Gaussians fp32 SH3 (64 clusters, seed 0), 1920x1080, 64-pose orbit "
+            "r=12 +-20deg; plain path at the reference's 16x16 tiles, batched path at the "
+            "autotuned tile size / digit width / raster batch (same image)")
 N_SPLATS, WIDTH, HEIGHT, TILE = 3_000_000, 1920, 1080, 16
 STAGES = ["preprocess-splats", "prefix-scan", "emit-tile-refs", "radix-sort",
           "identify-tile-ranges", "rasterize-tiles"]
@@ -131,6 +132,25 @@ def algorithmic_bytes(n, R, tiles, tile_passes, sh_floats, fused):
     }
 
 
+def install_cost_model(lib, ctx, tile):
+    """Cost model trained for this tile size, behind its gate; returns the
+    schedule to use and the model's held-out metrics (None when no model
+    exists for the tile size: key counts)."""
+    from gs3d import _lib, learned
+    path = learned.checkpoint_for(tile, tile)
+    if path is None:
+        return _lib.SCHEDULE_KEY_COUNT, None
+    mp, mmean, mstd, mmetrics, mbound = learned.load(path)
+    if not learned.gate(mmetrics, mbound):
+        return _lib.SCHEDULE_KEY_COUNT, mmetrics
+    f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    mp, mmean, mstd = f32(mp), f32(mmean), f32(mstd)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    if lib.gs3d_set_cost_model(ctx, ptr(mp), ptr(mmean), ptr(mstd)) != 0:
+        raise RuntimeError(lib.gs3d_last_error(ctx).decode())
+    return _lib.SCHEDULE_LEARNED, mmetrics
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -158,17 +178,12 @@ def run_ours(args, rank, world):
                               ptr(data.sphericalHarmonics), 3, 0))
     cam_structs = [camera_struct(u) for u in cams]
 
-    # cost model of the learned schedule, behind its gate (else key counts)
-    from gs3d import learned
-    mp, mmean, mstd, mmetrics, mbound = learned.load(
-        ROOT / "webgpu-3dgs_gb300" / "gs3d" / "cost_mlp_c1.npz")
-    use_learned = learned.gate(mmetrics, mbound)
-    f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
-    mp, mmean, mstd = f32(mp), f32(mmean), f32(mstd)
-    check(lib.gs3d_set_cost_model(ctx, ptr(mp), ptr(mmean), ptr(mstd)))
-    batched_schedule = _lib.SCHEDULE_LEARNED if use_learned else _lib.SCHEDULE_KEY_COUNT
+    def set_tuning(tile, digit_bits, raster_batch):
+        check(lib.gs3d_set_tuning(ctx, C.byref(_lib.Tuning_t(tile, tile, digit_bits,
+                                                              raster_batch))))
 
-    # first pass: size the key buffers (grow on overflow) and record ref counts
+    # first pass at the reference's 16x16 tiles: size the key buffers and
+    # record the per-view ref counts
     refs = []
     for cs in cam_structs:
         for _ in range(3):
@@ -191,6 +206,28 @@ def run_ours(args, rank, world):
             arr[i].width, arr[i].height = WIDTH, HEIGHT
         batches.append(arr)
 
+    # autotuner over the first batch (tile size, digit width, raster batch);
+    # every candidate renders the same image
+    tune_out = (_lib.TuneResult_t * 64)()
+    n_tuned = C.c_uint32()
+    check(lib.gs3d_set_flags(ctx, _lib.FLAG_CUDA_GRAPH))
+    check(lib.gs3d_autotune(ctx, C.cast(batches[0], C.c_void_p), len(batches[0]), 2, tune_out,
+                            64, C.byref(n_tuned)))
+    check(lib.gs3d_set_flags(ctx, 0))
+    tuned = _lib.Tuning_t()
+    check(lib.gs3d_get_tuning(ctx, C.byref(tuned)))
+    tune_table = sorted(({"tile": r.tuning.tile_w, "digit_bits": r.tuning.digit_bits,
+                          "raster_batch": r.tuning.raster_batch,
+                          "ms_per_view": round(float(r.ms_per_view), 4),
+                          "tile_passes": int(r.tile_passes)}
+                         for r in tune_out[:n_tuned.value]), key=lambda r: r["ms_per_view"])
+    best = next(r for r in tune_out[:n_tuned.value]
+                if (r.tuning.tile_w, r.tuning.digit_bits, r.tuning.raster_batch) ==
+                (tuned.tile_w, tuned.digit_bits, tuned.raster_batch))
+    tuned_R = best.refs / len(batches[0])
+    tuned_passes = int(best.tile_passes)
+    batched_schedule, tuned_model = install_cost_model(lib, ctx, tuned.tile_w)
+
     def run_step(path):
         if path == "batched":
             for arr in batches:
@@ -199,12 +236,10 @@ def run_ours(args, rank, world):
             for cs in cam_structs:
                 check(lib.gs3d_rebin(ctx, C.byref(cs), WIDTH, HEIGHT))
 
-    def timed(path: str, schedule=None, graph=False):
+    def timed(path: str, schedule, graph=False):
         flags = (_lib.FLAG_CUDA_GRAPH if graph else _lib.FLAG_STAGE_TIMING) | \
             (_lib.FLAG_STAGEWISE_REBIN if path == "stagewise" else 0)
         check(lib.gs3d_set_flags(ctx, flags))
-        if schedule is None:
-            schedule = batched_schedule if path == "batched" else _lib.SCHEDULE_ROW_MAJOR
         check(lib.gs3d_set_schedule(ctx, schedule))
         for _ in range(3):  # size the key buffers for this path's batch
             run_step(path)
@@ -243,48 +278,60 @@ def run_ours(args, rank, world):
         return total, per_stage, clocks.summary()
 
     views = args.steps * len(cam_structs)
-    batched_ms, _, clocks = timed("batched", graph=True)       # headline: CUDA graph replays
-    eager_ms, batched_stages, _ = timed("batched")              # same work, per-stage events
-    fused_ms, fused_stages, _ = timed("fused")
-    stagewise_ms, stagewise_stages, _ = timed("stagewise")
-    # the raster under each work order (single-view fused path); images are identical
-    sched_raster = {}
-    for name, sc in (("row_major", _lib.SCHEDULE_ROW_MAJOR), ("key_count", _lib.SCHEDULE_KEY_COUNT),
-                     ("learned", _lib.SCHEDULE_LEARNED)):
-        ms_, st_, _ = timed("fused", sc)
-        sched_raster[name] = {"raster_ms": round(st_["rasterize-tiles"][0], 4),
-                              "views_per_s": round(views * world / (ms_ * 1e-3), 1)}
-    views = args.steps * len(cam_structs)
+    # headline: batched, autotuned, learned schedule, CUDA graph replays
+    batched_ms, _, clocks = timed("batched", batched_schedule, graph=True)
+    eager_ms, batched_stages, _ = timed("batched", batched_schedule)  # per-stage events
 
-    # ---- e2e: public entry point, host camera in, pinned host image out ----
+    # ---- e2e: the public batched entry point with host view tables in and
+    # pinned host images out, every batch, under the same tuning ----
     img_bytes = WIDTH * HEIGHT * 8
-    pinned = torch.empty(img_bytes * 2, dtype=torch.uint8, pin_memory=True)
+    batch_bytes = img_bytes * B
+    pinned = torch.empty(batch_bytes * 2, dtype=torch.uint8, pin_memory=True)
+    check(lib.gs3d_set_flags(ctx, _lib.FLAG_CUDA_GRAPH))
+    check(lib.gs3d_set_schedule(ctx, batched_schedule))
     for _ in range(2):
-        check(lib.gs3d_rebin(ctx, C.byref(cam_structs[0]), WIDTH, HEIGHT))
+        run_step("batched")
     check(lib.gs3d_synchronize(ctx))
     t0 = time.perf_counter()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for k in range(args.steps):
-        for v in range(len(cams)):
-            cs = camera_struct(cams[v])  # host struct built per view
-            check(lib.gs3d_rebin(ctx, C.byref(cs), WIDTH, HEIGHT))
-            check(lib.gs3d_copy_buffer_async(ctx, 14, C.c_void_p(pinned.data_ptr() +
-                                                                  (v % 2) * img_bytes), img_bytes))
+        for bi, arr in enumerate(batches):
+            for i in range(len(arr)):  # host view table built per batch
+                arr[i].camera = camera_struct(cams[bi * B + i])
+            check(lib.gs3d_rebin_batch(ctx, C.cast(arr, C.c_void_p), len(arr)))
+            check(lib.gs3d_copy_buffer_async(
+                ctx, 14, C.c_void_p(pinned.data_ptr() + (bi % 2) * batch_bytes),
+                img_bytes * len(arr)))
     e1.record(stream)
     check(lib.gs3d_synchronize(ctx))
     e2e_wall = time.perf_counter() - t0
     e2e_ms = e0.elapsed_time(e1)
+    check(lib.gs3d_set_flags(ctx, 0))
+
+    # ---- reference tuning (16x16 tiles, 8-bit digits, one splat per pixel
+    # per raster batch): single-view fused, the plain stage-wise path and the
+    # raster under each work order ----
+    set_tuning(TILE, 8, 0)
+    sched16, model16 = install_cost_model(lib, ctx, TILE)
+    fused_ms, fused_stages, _ = timed("fused", _lib.SCHEDULE_ROW_MAJOR)
+    stagewise_ms, stagewise_stages, _ = timed("stagewise", _lib.SCHEDULE_ROW_MAJOR)
+    sched_raster = {}
+    for name, sc in (("row_major", _lib.SCHEDULE_ROW_MAJOR), ("key_count", _lib.SCHEDULE_KEY_COUNT),
+                     ("learned", sched16)):
+        ms_, st_, _ = timed("fused", sc)
+        sched_raster[name] = {"raster_ms": round(st_["rasterize-tiles"][0], 4),
+                              "views_per_s": round(views * world / (ms_ * 1e-3), 1)}
     lib.gs3d_destroy(ctx)
 
-    tiles = (WIDTH // TILE) * -(-HEIGHT // TILE)
-    tile_passes = ((tiles - 1).bit_length() + 7) // 8          # one view
-    batch_tile_passes = ((tiles * B - 1).bit_length() + 7) // 8  # B views: global tile ids
+    tiles16 = -(-WIDTH // TILE) * -(-HEIGHT // TILE)
+    tile_passes16 = ((tiles16 - 1).bit_length() + 7) // 8
+    tiles_t = -(-WIDTH // tuned.tile_w) * -(-HEIGHT // tuned.tile_h)
     mean_R = float(np.mean(refs))
     peak, peak_kind = peaks()
 
-    def roof(stages, fused, passes=tile_passes):
-        algo = algorithmic_bytes(N_SPLATS, mean_R, tiles, passes, 45, fused)
+    def roof(stages, fused, R, tiles, passes, tile_px):
+        algo = algorithmic_bytes(N_SPLATS, R, tiles, passes, 45, fused)
         out = {}
         for name, (ms, n) in stages.items():
             gbs = algo[name] / (ms * 1e-3) / 1e9
@@ -292,28 +339,32 @@ def run_ours(args, rank, world):
                          "frac_hbm": round(gbs / peak, 3)}
         return out
 
-    batched_roof = roof(batched_stages, True, batch_tile_passes)
+    batched_roof = roof(batched_stages, True, tuned_R, tiles_t, tuned_passes, tuned.tile_w)
     hbm = [s for s in batched_roof if s != "rasterize-tiles"]
     dom = max(hbm, key=lambda s: batched_roof[s]["ms"])
+    learned_on = batched_schedule == _lib.SCHEDULE_LEARNED
     # kernels of one batched rebin: preprocess, depth sort (histogram + 4 passes), scan, emit,
     # tile-digit passes, identify, schedule (features + MLP + keys + histogram + 2 passes
     # for the learned one; keys + histogram + 2 passes for key counts), raster
-    launches_per_batch = 1 + 5 + 1 + 1 + batch_tile_passes + 1 + (6 if use_learned else 4) + 1
+    launches_per_batch = 1 + 5 + 1 + 1 + tuned_passes + 1 + (6 if learned_on else 4) + 1
     return {
         "value": views * world / (batched_ms * 1e-3), "ms_per_step": batched_ms / args.steps,
         "views": views, "per_stage": batched_roof, "dominant": dom, "peak": peak,
-        "fused_value": views * world / (fused_ms * 1e-3), "fused_stages": roof(fused_stages, True),
+        "fused_value": views * world / (fused_ms * 1e-3),
+        "fused_stages": roof(fused_stages, True, mean_R, tiles16, tile_passes16, TILE),
         "batched_eager_value": views * world / (eager_ms * 1e-3),
-        "peak_kind": peak_kind, "mean_refs": mean_R, "tile_passes": tile_passes,
+        "peak_kind": peak_kind, "mean_refs": mean_R, "tuned_refs": tuned_R,
         "clocks": clocks,
         "stagewise_value": views * world / (stagewise_ms * 1e-3),
-        "stagewise_stages": roof(stagewise_stages, False),
+        "stagewise_stages": roof(stagewise_stages, False, mean_R, tiles16, tile_passes16, TILE),
         "e2e_value": views * world / (e2e_ms * 1e-3), "e2e_wall_value": views / e2e_wall,
-        "h2d": 288 * len(cam_structs), "d2h": img_bytes * len(cam_structs),
+        "h2d": 416 * len(cam_structs), "d2h": img_bytes * len(cam_structs),
         "launches_per_step": launches_per_batch * len(batches),
-        "schedules": sched_raster, "learned_active": use_learned,
-        "cost_model": {k: round(v, 4) for k, v in mmetrics.items()},
-        "tile_passes_batched": batch_tile_passes,
+        "schedules": sched_raster, "learned_active": learned_on,
+        "cost_model": {k: round(v, 4) for k, v in (tuned_model or {}).items()},
+        "tuning": {"tile": tuned.tile_w, "digit_bits": tuned.digit_bits,
+                   "raster_batch": tuned.raster_batch, "candidates": tune_table},
+        "tile_passes_batched": tuned_passes,
     }
 
 
@@ -331,14 +382,11 @@ def profile_run(args):
     assert lib.gs3d_set_splats(ctx, data.splatCount, ptr(data.positions), ptr(data.scales),
                                ptr(data.rotations), ptr(data.colors),
                                ptr(data.sphericalHarmonics), 3, 0) == 0
-    from gs3d import learned
-    mp, mmean, mstd, mmetrics, mbound = learned.load(
-        ROOT / "webgpu-3dgs_gb300" / "gs3d" / "cost_mlp_c1.npz")
-    f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
-    mp, mmean, mstd = f32(mp), f32(mmean), f32(mstd)
-    assert lib.gs3d_set_cost_model(ctx, ptr(mp), ptr(mmean), ptr(mstd)) == 0
-    assert lib.gs3d_set_schedule(ctx, _lib.SCHEDULE_LEARNED if learned.gate(mmetrics, mbound)
-                                 else _lib.SCHEDULE_KEY_COUNT) == 0
+    tile, digit_bits, raster_batch = (int(x) for x in args.tuning.split(","))
+    assert lib.gs3d_set_tuning(ctx, C.byref(_lib.Tuning_t(tile, tile, digit_bits,
+                                                           raster_batch))) == 0
+    schedule, _ = install_cost_model(lib, ctx, tile)
+    assert lib.gs3d_set_schedule(ctx, schedule) == 0
     B = args.batch
     for step in range(args.profile):
         for b0 in range(0, len(cams), B):
@@ -383,6 +431,8 @@ def main():
     ap.add_argument("--profile", type=int, default=0, metavar="STEPS",
                     help="profiling run: render STEPS batched steps of --views views and exit "
                          "(no timing, no JSON)")
+    ap.add_argument("--tuning", default=f"{TILE},8,0", metavar="TILE,DIGIT_BITS,RASTER_BATCH",
+                    help="profiling run: the tuning to render with (the bench autotunes)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -428,10 +478,12 @@ def main():
             "data": "synthetic",
             "config": {"workload": WORKLOAD,
                        "path": f"batched fused rebin, {args.batch} views per launch sequence, "
-                               "replayed as a CUDA graph",
+                               "autotuned, replayed as a CUDA graph",
+                       "tuning": res["tuning"],
+                       "mean_refs_per_view_tuned": res["tuned_refs"],
                        "batched_without_graph_views_per_s": res["batched_eager_value"],
                        "views_per_step": args.views, "l2": "inputs larger than L2 (no flush)",
-                       "mean_refs_per_view": res["mean_refs"],
+                       "mean_refs_per_view_16x16": res["mean_refs"],
                        "tile_digit_passes": res["tile_passes_batched"],
                        "single_view_fused_views_per_s": res["fused_value"],
                        "raster_schedule": "learned (cost MLP)" if res["learned_active"]

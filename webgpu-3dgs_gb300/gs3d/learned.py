@@ -184,10 +184,21 @@ def load(path) -> tuple[np.ndarray, np.ndarray, np.ndarray, dict, float]:
     return d["params"], d["mean"], d["std"], metrics, float(d["bound"])
 
 
+def checkpoint_for(tile_w: int, tile_h: int):
+    """Committed cost model of the 3M-splat 1080p workload for a tile size,
+    or None (the model's features and costs are per tile, so a model only
+    applies to the tile size it was trained on)."""
+    from pathlib import Path
+    here = Path(__file__).resolve().parent
+    name = {(16, 16): "cost_mlp_c1.npz", (32, 32): "cost_mlp_c1_t32.npz"}.get((tile_w, tile_h))
+    return here / name if name and (here / name).exists() else None
+
+
 def main(argv=None) -> None:
     """Trains the cost model of the headline workload (3M-splat cluster
-    scene, 1920x1080, 16x16 tiles) on random poses at radius 8-16 and writes
-    the checkpoint:  python -m gs3d.learned OUT.npz [--poses 10000] [--heldout 1000]"""
+    scene, 1920x1080, 16x16 tiles by default) on random poses at radius
+    8-16 and writes the checkpoint:
+    python -m gs3d.learned OUT.npz [--poses 10000] [--heldout 1000] [--tile 16]"""
     import argparse
     import time
 
@@ -205,9 +216,11 @@ def main(argv=None) -> None:
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--steps", type=int, default=6000)
     ap.add_argument("--chunk", type=int, default=1000)
+    ap.add_argument("--tile", type=int, default=16)
     a = ap.parse_args(argv)
     r = GaussianSplatRenderer(Scene())
     r.init()
+    r.setTileSize(a.tile, a.tile)
     # colour does not change a tile's raster cost: SH degree 0 suffices
     r.setSplatData(scenes.scene_clusters(a.splats, seed=0, sh_degree=0))
     total = a.poses + a.heldout
@@ -231,7 +244,8 @@ def main(argv=None) -> None:
     ok = gate(m)
     print(f"collect {t_collect:.1f}s train {t_train:.1f}s held-out {m} gate {'pass' if ok else 'FAIL'}")
     save(a.out, res, m, poses=np.int64(a.poses), heldout=np.int64(a.heldout),
-         workload=np.array(f"{a.splats} splats {a.width}x{a.height} tiles 16x16"))
+         workload=np.array(f"{a.splats} splats {a.width}x{a.height} tiles {a.tile}x{a.tile}"),
+         tile=np.int64(a.tile))
     r.destroy()
 
 
