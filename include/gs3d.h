@@ -306,6 +306,42 @@ int gs3d_mlp_infer(const float* params, const float* x, uint32_t n, float* y, vo
  * ref count; re-issue the rebin. */
 int gs3d_synchronize(struct gs3d_ctx* ctx);
 
+/* ---- PLY ingest (SceneWorker.ts:146-550) ------------------------------------- */
+
+#define GS3D_PLY_ASCII      0u
+#define GS3D_PLY_BINARY_LE  1u
+#define GS3D_PLY_BINARY_BE  2u
+#define GS3D_PLY_NEW_SCENE  0xffffffffu  /* gs3d_load_ply target: add a scene */
+
+typedef struct gs3d_ply_info {
+    uint64_t splat_count;     /* vertex rows                                          */
+    uint64_t header_bytes;    /* through the newline after end_header                 */
+    uint32_t format;          /* GS3D_PLY_*                                           */
+    uint32_t f_rest_count;    /* f_rest_* properties of the vertex element            */
+    uint32_t sh_degree;       /* inferred from f_rest_count (SceneWorker.ts:501-506)  */
+    uint32_t vertex_stride;   /* bytes per binary vertex row (0 for ASCII)            */
+    float bounds_min[3];      /* position bounds (gs3d_load_ply only)                 */
+    float bounds_max[3];
+} gs3d_ply_info;
+
+/* Parses and validates the header of a Gaussian-splat PLY held in host
+ * memory (no device, no context): formats ascii / binary_little_endian /
+ * binary_big_endian, the 14 required vertex properties, no list properties.
+ * Errors: GS3D_ERR_INVALID_ARG with the reference's message in
+ * gs3d_last_error(NULL). */
+int gs3d_ply_inspect(const void* data, size_t size, gs3d_ply_info* out);
+
+/* Loads a Gaussian-splat PLY (host memory) into the context: the vertex rows
+ * are copied to the device and decoded and activated there (positions, colors
+ * = clamp01(0.5 + C0 f_dc) and clamp01(sigmoid(opacity)), scales = exp,
+ * rotations normalised, computed in f64 and rounded to f32; f_rest kept in
+ * file order).  target 0 replaces the gs3d_set_splats scene;
+ * GS3D_PLY_NEW_SCENE adds a scene (its id in *out_scene).  SH is used for
+ * colour when the f_rest count is 3 * ((d+1)^2 - 1) for the inferred degree
+ * d, or a larger multiple of 3 (the first coefficients of each channel). */
+int gs3d_load_ply(struct gs3d_ctx* ctx, const void* data, size_t size, uint32_t target,
+                  uint32_t* out_scene, gs3d_ply_info* info);
+
 /* ---- buffer access ---------------------------------------------------------- */
 
 /* Device pointer and size in bytes of a named buffer (for zero-copy callers). */

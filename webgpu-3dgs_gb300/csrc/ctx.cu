@@ -805,6 +805,110 @@ int gs3d_add_scene(gs3d_ctx* c, uint32_t n, const float* positions, const float*
   return GS3D_OK;
 }
 
+int gs3d_load_ply(gs3d_ctx* c, const void* data, size_t size, uint32_t target,
+                  uint32_t* out_scene, gs3d_ply_info* info) {
+  if (!c || !data) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
+  if (target != 0 && target != GS3D_PLY_NEW_SCENE)
+    return fail(c, GS3D_ERR_INVALID_ARG, "target must be 0 or GS3D_PLY_NEW_SCENE");
+  TRY(set_device(c));
+  const uint8_t* bytes = static_cast<const uint8_t*>(data);
+  PlyLayout lay;
+  std::string err;
+  if (!ply_parse_layout(bytes, size, &lay, &err))
+    return fail(c, GS3D_ERR_INVALID_ARG, "%s", err.c_str());
+  const uint8_t* rows = bytes + lay.rows_offset;
+  std::vector<double> ascii;
+  if (lay.format == GS3D_PLY_ASCII) {
+    if (!ply_ascii_rows(bytes, size, lay, &ascii, &err))
+      return fail(c, GS3D_ERR_INVALID_ARG, "%s", err.c_str());
+    rows = reinterpret_cast<const uint8_t*>(ascii.data());
+  }
+  const uint32_t n = (uint32_t)lay.count;
+  const uint32_t deg = lay.sh_k ? lay.sh_degree : 0u;
+  SceneBufs fresh;
+  SceneBufs& sc = target == 0 ? c->scenes[0] : fresh;
+  const size_t v4 = (size_t)n * 16;
+  DevBuf d_rows, d_words;
+  auto cleanup = [&](int rc) {
+    release(d_rows);
+    release(d_words);
+    if (&sc == &fresh) {
+      release(fresh.pos);
+      release(fresh.scale);
+      release(fresh.rot);
+      release(fresh.color);
+      release(fresh.sh);
+    }
+    return rc;
+  };
+  int rc = GS3D_OK;
+  if ((rc = ensure(c, sc.pos, v4, "splat_positions")) || (rc = ensure(c, sc.scale, v4, "splat_scales")) ||
+      (rc = ensure(c, sc.rot, v4, "splat_rotations")) || (rc = ensure(c, sc.color, v4, "splat_colors")) ||
+      (lay.sh_k && (rc = ensure(c, sc.sh, (size_t)n * 3 * lay.sh_k * sizeof(float), "splat_sh_rest"))) ||
+      (rc = ensure(c, d_rows, std::max<size_t>((size_t)n * lay.stride, 16), "ply rows")) ||
+      (rc = ensure(c, d_words, 64, "ply status")))
+    return cleanup(rc);
+  uint32_t words[7] = {0u, 0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+  cudaError_t e = cudaMemcpyAsync(d_words.p, words, sizeof(words), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess && n)
+    e = cudaMemcpyAsync(d_rows.p, rows, (size_t)n * lay.stride, cudaMemcpyHostToDevice, c->stream);
+  uint32_t* dw = static_cast<uint32_t*>(d_words.p);
+  if (e == cudaSuccess)
+    e = launch_ply_decode(static_cast<const uint8_t*>(d_rows.p), n, lay,
+                          lay.format == GS3D_PLY_BINARY_BE, static_cast<float4*>(sc.pos.p),
+                          static_cast<float4*>(sc.scale.p), static_cast<float4*>(sc.rot.p),
+                          static_cast<float4*>(sc.color.p), static_cast<float*>(sc.sh.p), dw,
+                          dw + 1, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(words, d_words.p, sizeof(words), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cleanup(cuda_fail(c, e, "ply decode"));
+  if (words[0] != 0)
+    return cleanup(fail(c, GS3D_ERR_INVALID_ARG, "Invalid Gaussian Splat PLY row: missing '%s'",
+                        ply_required_name((int)words[0] - 1)));
+  release(d_rows);
+  release(d_words);
+  sc.n = n;
+  sc.sh_degree = deg;
+  if (&sc == &fresh) {
+    if (!c->have_scene) {
+      c->scenes[0] = fresh;
+      if (out_scene) *out_scene = 0;
+    } else {
+      c->scenes.push_back(fresh);
+      if (out_scene) *out_scene = (uint32_t)c->scenes.size() - 1;
+    }
+  } else {
+    if (out_scene) *out_scene = 0;
+    TRY(ensure_splat_buffers(c, n));
+    TRY(ensure_key_capacity(
+        c, std::min<uint64_t>((uint64_t)std::max<uint32_t>(n, 1) * c->max_tiles_per_splat,
+                              kMaxCapacity)));
+    c->have_camera = false;
+  }
+  c->have_scene = true;
+  if (info) {
+    *info = gs3d_ply_info{};
+    info->splat_count = lay.count;
+    info->header_bytes = lay.header_bytes;
+    info->format = lay.format;
+    info->f_rest_count = lay.f_rest_count;
+    info->sh_degree = lay.sh_degree;
+    info->vertex_stride = lay.format == GS3D_PLY_ASCII ? 0u : lay.stride;
+    auto unord = [](uint32_t o) {
+      const uint32_t u = (o & 0x80000000u) ? (o & 0x7fffffffu) : ~o;
+      float f;
+      std::memcpy(&f, &u, 4);
+      return f;
+    };
+    for (int k = 0; k < 3; ++k) {
+      info->bounds_min[k] = n ? unord(words[1 + k]) : 0.0f;
+      info->bounds_max[k] = n ? unord(words[4 + k]) : 0.0f;
+    }
+  }
+  return GS3D_OK;
+}
+
 int gs3d_set_tile_size(gs3d_ctx* c, uint32_t tx, uint32_t ty, uint32_t* out_x, uint32_t* out_y) {
   if (!c) return GS3D_ERR_INVALID_ARG;
   // clampTileSize (GaussianSplatRenderer.ts:162-167) with CUDA's 1024-thread block limit

@@ -6,6 +6,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+#include <vector>
+
 #include "../../include/gs3d.h"
 
 namespace gs3d {
@@ -221,6 +224,8 @@ cudaError_t launch_scan(const uint32_t* counts, const uint32_t* gather, uint32_t
 size_t scan_status_words(uint32_t n);
 // Message of the calling thread's last failing context-free call.
 const char* noalloc_last_error();
+// Sets the message gs3d_last_error(NULL) returns on the calling thread.
+void set_context_free_error(const char* msg);
 // Emit in splat order (the reference's emit_tile_refs, one view).
 cudaError_t launch_emit(const FrameUniforms* d_frame, uint32_t n,
                         const gs3d_projected_splat* proj, const uint32_t* offsets,
@@ -312,5 +317,44 @@ struct RasterArgs {
   bool culled;
 };
 cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s);
+
+// ---- PLY ingest (ply.cu) ----------------------------------------------------
+enum PlyScalar : uint32_t { PLY_I8, PLY_U8, PLY_I16, PLY_U16, PLY_I32, PLY_U32, PLY_F32, PLY_F64 };
+struct PlyField {
+  uint32_t offset;  // byte offset within a vertex row
+  uint32_t type;    // PlyScalar
+};
+constexpr int kPlyRequired = 14;  // x y z opacity scale_0..2 rot_0..3 f_dc_0..2
+constexpr int kPlyMaxRest = 45;
+// Where the vertex rows of a parsed PLY are and how to read them.  ASCII
+// bodies are converted on the host into little-endian f64 rows first.
+struct PlyLayout {
+  uint64_t count = 0;          // vertex rows
+  uint64_t rows_offset = 0;    // byte offset of the first vertex row (binary)
+  uint64_t header_bytes = 0;
+  uint32_t stride = 0;         // bytes per vertex row
+  uint32_t format = 0;         // GS3D_PLY_*
+  uint32_t f_rest_count = 0;   // f_rest_* properties
+  uint32_t sh_degree = 0;      // inferred from f_rest_count
+  PlyField req[kPlyRequired];
+  uint32_t sh_k = 0;           // SH coefficients per channel used for colour (0: none)
+  PlyField rest[kPlyMaxRest];  // the used f_rest fields, [channel][coefficient]
+  uint32_t vertex_props = 0;   // properties per vertex row
+};
+const char* ply_required_name(int k);
+// Parses the header and lays out the vertex element (host only).  On error
+// returns false with the message in *err.
+bool ply_parse_layout(const uint8_t* data, size_t size, PlyLayout* out, std::string* err);
+// Tokenizes an ASCII body into count x vertex_props f64 values (host only).
+bool ply_ascii_rows(const uint8_t* data, size_t size, const PlyLayout& lay,
+                    std::vector<double>* rows, std::string* err);
+// Decodes n vertex rows on the device into the four vec4 SoA arrays and the
+// SH block (lay.sh_k coefficients per channel, channel-major), activating as
+// the reference's loader does; the first non-finite required value latches
+// 1 + its field index in *bad; bounds = 6 ordered-u32 words (min xyz, max xyz).
+cudaError_t launch_ply_decode(const uint8_t* rows, uint64_t n, const PlyLayout& lay,
+                              bool big_endian, float4* pos, float4* scale,
+                              float4* rot, float4* color, float* sh, uint32_t* bad,
+                              uint32_t* bounds, cudaStream_t s);
 
 }  // namespace gs3d

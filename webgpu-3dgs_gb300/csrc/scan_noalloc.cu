@@ -45,6 +45,7 @@ int fail(int code, const char* msg) {
 
 namespace gs3d {
 const char* noalloc_last_error() { return g_error; }
+void set_context_free_error(const char* msg) { snprintf(g_error, sizeof(g_error), "%s", msg); }
 }  // namespace gs3d
 
 extern "C" int gs3d_prefix_scan_noalloc(const uint32_t* counts, uint32_t* offsets, uint32_t n,

@@ -76,6 +76,16 @@ class TuneResult_t(C.Structure):
                 ("refs", C.c_uint64)]
 
 
+class PlyInfo_t(C.Structure):
+    _fields_ = [("splat_count", C.c_uint64), ("header_bytes", C.c_uint64),
+                ("format", C.c_uint32), ("f_rest_count", C.c_uint32),
+                ("sh_degree", C.c_uint32), ("vertex_stride", C.c_uint32),
+                ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3)]
+
+
+PLY_NEW_SCENE = 0xFFFFFFFF
+
+
 class ViewInfo_t(C.Structure):
     _fields_ = [("pixel_offset", C.c_uint64), ("width", C.c_uint32), ("height", C.c_uint32),
                 ("tiles_x", C.c_uint32), ("tiles_y", C.c_uint32), ("tile_base", C.c_uint32),
@@ -124,6 +134,8 @@ SIGNATURES = {
     "gs3d_ref_count": ([_P, C.POINTER(_U32)], _I),
     "gs3d_read_tile_counts": ([_P, _P, _SZ], _I),
     "gs3d_prefix_scan_noalloc": ([_P, _P, _U32, _P], _I),
+    "gs3d_ply_inspect": ([_P, _SZ, C.POINTER(PlyInfo_t)], _I),
+    "gs3d_load_ply": ([_P, _P, _SZ, _U32, C.POINTER(_U32), C.POINTER(PlyInfo_t)], _I),
     "gs3d_set_cost_model": ([_P, _P, _P, _P], _I),
     "gs3d_tile_features": ([_P, _P, _P, _U32, _I], _I),
     "gs3d_mlp_forward": ([_P, _P, _U32, _P, _P, _P], _I),

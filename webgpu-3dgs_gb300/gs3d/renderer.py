@@ -268,6 +268,27 @@ class GaussianSplatRenderer:
             return
         _check(self.lib, self.ctx, rc)
 
+    def loadPly(self, source, newScene: bool = False) -> tuple[int, dict]:
+        """SceneLoader.startLoadSplats + SceneWorker.parseGaussianSplatPly
+        (SceneLoader.ts:75-88, SceneWorker.ts:146-550): parses the PLY at
+        `source` (a path or bytes) and decodes it on the device into the
+        scene (scene 0, like setSplatData, or a new scene for batched views).
+        Returns (scene id, header info with position bounds)."""
+        from . import ply
+        if isinstance(source, (bytes, bytearray, memoryview)):
+            data = np.frombuffer(source, np.uint8)
+        else:
+            data = np.fromfile(source, np.uint8)
+        info = _lib.PlyInfo_t()
+        out = C.c_uint32()
+        self._call("gs3d_load_ply", data.ctypes.data_as(C.c_void_p), data.nbytes,
+                   _lib.PLY_NEW_SCENE if newScene else 0, C.byref(out), C.byref(info))
+        d = ply.info_dict(info)
+        if not newScene or self.scene.splats is None:
+            self.scene.splats = DeviceSplats(d["splat_count"], d["sh_degree"])
+            self.lastSplatCount = -1  # force a rebin
+        return int(out.value), d
+
     # ---- batched rendering (extension) -----------------------------------------
     def addScene(self, data: GaussianSplatData) -> int:
         """Makes another scene resident; returns its id for batched views."""
@@ -387,7 +408,11 @@ class GaussianSplatRenderer:
         w, h = self.viewport
         if name in ("sort_keys_a", "sort_values_a", "sort_keys_b", "sort_values_b"):
             count = self.refCount() if count is None else count
+        deg = self.scene.splats.sphericalHarmonicsDegree if self.scene.splats else 0
         shapes = {
+            "splat_positions": (np.float32, (n, 4)), "splat_scales": (np.float32, (n, 4)),
+            "splat_rotations": (np.float32, (n, 4)), "splat_colors": (np.float32, (n, 4)),
+            "splat_sh_rest": (np.float32, (n, 3 * ((deg + 1) ** 2 - 1))),
             "projected_splats": (PROJ_DTYPE, (n,)),
             "splat_ref_counts": (np.uint32, (n,)),
             "splat_ref_offsets": (np.uint32, (n + 1,)),
@@ -418,6 +443,14 @@ class GaussianSplatRenderer:
         out = np.zeros(tiles, np.uint32)
         self._call("gs3d_read_tile_counts", out.ctypes.data_as(C.c_void_p), tiles)
         return out
+
+
+class DeviceSplats:
+    """A scene whose splat arrays live only on the device (loadPly)."""
+
+    def __init__(self, count: int, sh_degree: int):
+        self.splatCount = int(count)
+        self.sphericalHarmonicsDegree = int(sh_degree)
 
 
 class SceneSyncer:

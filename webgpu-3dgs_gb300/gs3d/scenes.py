@@ -66,16 +66,22 @@ def _normal(rng, size, mean=0.0, std=1.0):
             + np.float32(mean)).astype(np.float32)
 
 
-def scene_small(n: int = 100_000, seed: int = 0) -> GaussianSplatData:
-    """100k splats, SH degree 0: pos N(0, 1.5^2), scale exp(N(-4.5, 0.8^2)),
-    rotation normalised N(0, 1)^4, opacity sigmoid(N(0, 1.5^2)), f_dc N(0, 0.5^2)."""
+def raw_small(n: int = 100_000, seed: int = 0) -> dict:
+    """Raw (PLY) values of scene_small."""
     rng = np.random.default_rng(seed)
     xyz = _normal(rng, (n, 3), 0.0, 1.5)
     scale_log = _normal(rng, (n, 3), -4.5, 0.8)
     rot = _normal(rng, (n, 4))
     opacity = _normal(rng, n, 0.0, 1.5)
     f_dc = _normal(rng, (n, 3), 0.0, 0.5)
-    return activate(xyz, f_dc, opacity, scale_log, rot)
+    return dict(xyz=xyz, f_dc=f_dc, opacity=opacity, scale_log=scale_log, rot=rot, f_rest=None,
+                sh_degree=0)
+
+
+def scene_small(n: int = 100_000, seed: int = 0) -> GaussianSplatData:
+    """100k splats, SH degree 0: pos N(0, 1.5^2), scale exp(N(-4.5, 0.8^2)),
+    rotation normalised N(0, 1)^4, opacity sigmoid(N(0, 1.5^2)), f_dc N(0, 0.5^2)."""
+    return activate(**raw_small(n, seed))
 
 
 def scene_clusters(n: int = 3_000_000, seed: int = 0, sh_degree: int = 3,
@@ -83,6 +89,12 @@ def scene_clusters(n: int = 3_000_000, seed: int = 0, sh_degree: int = 3,
     """Mixture of isotropic clusters (centres uniform in a radius-8 ball,
     sigma ~ U(0.2, 1.5)), scale exp(N(-4, 1)), rotation/opacity as the small
     scene, f_dc N(0, 0.5^2), f_rest N(0, 0.1^2)."""
+    return activate(**raw_clusters(n, seed, sh_degree, clusters))
+
+
+def raw_clusters(n: int = 3_000_000, seed: int = 0, sh_degree: int = 3,
+                 clusters: int = 64) -> dict:
+    """Raw (PLY) values of scene_clusters."""
     rng = np.random.default_rng(seed)
     d = rng.standard_normal((clusters, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
@@ -96,7 +108,8 @@ def scene_clusters(n: int = 3_000_000, seed: int = 0, sh_degree: int = 3,
     f_dc = _normal(rng, (n, 3), 0.0, 0.5)
     k = 3 * ((sh_degree + 1) ** 2 - 1)
     f_rest = _normal(rng, (n, k), 0.0, 0.1) if k else None
-    return activate(xyz, f_dc, opacity, scale_log, rot, f_rest, sh_degree)
+    return dict(xyz=xyz, f_dc=f_dc, opacity=opacity, scale_log=scale_log, rot=rot, f_rest=f_rest,
+                sh_degree=sh_degree)
 
 
 def scene_skewed(n: int = 10_000_000, seed: int = 0, sh_degree: int = 3) -> GaussianSplatData:
