@@ -342,6 +342,23 @@ int gs3d_ply_inspect(const void* data, size_t size, gs3d_ply_info* out);
 int gs3d_load_ply(struct gs3d_ctx* ctx, const void* data, size_t size, uint32_t target,
                   uint32_t* out_scene, gs3d_ply_info* info);
 
+/* ---- headless composite (render passes after the rasterizer) ------------------ */
+
+#define GS3D_COMPOSITE_SPLATS       0u  /* composite_splats.wgsl                       */
+#define GS3D_COMPOSITE_TILE_HEATMAP 1u  /* debug_tile_overlay.wgsl, then the composite */
+
+/* Composites view `view` of the last rebin over `background` (premultiplied
+ * rgba; the reference's framebuffer holds the grid pass there) with the
+ * premultiplied "over" blend of the composite pass, into width x height RGBA8
+ * pixels (round(clamp01(x) * 255), row-major, top row first).  Mode
+ * GS3D_COMPOSITE_TILE_HEATMAP first tints each tile green -> red by its key
+ * count / debug_ref (0 -> 256, GaussianSplatRenderer.ts:75) at 40% opacity,
+ * through an rgba16float target as the overlay pass does.  memory: 0 = host
+ * destination (blocking), 1 = device destination (stream ordered).  `bytes`
+ * must be at least width * height * 4. */
+int gs3d_composite(struct gs3d_ctx* ctx, uint32_t view, uint32_t mode, uint32_t debug_ref,
+                   const float background[4], void* rgba8, size_t bytes, int memory);
+
 /* ---- buffer access ---------------------------------------------------------- */
 
 /* Device pointer and size in bytes of a named buffer (for zero-copy callers). */

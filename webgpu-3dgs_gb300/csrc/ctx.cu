@@ -78,7 +78,7 @@ struct gs3d_ctx {
   DevBuf scan_status, sort_status;
   uint32_t scan_epoch = 0;
   DevBuf depth_keys_a, depth_ids_a, depth_keys_b, depth_ids_b, sorted_offsets, depth_status;
-  DevBuf tile_offsets, image, tile_costs;
+  DevBuf tile_offsets, image, tile_costs, composite_out;
   DevBuf sched_keys_a, sched_keys_b, sched_order_a, sched_order_b, sched_status;
   // cost model (learned schedule)
   bool have_model = false;
@@ -748,7 +748,7 @@ int gs3d_destroy(gs3d_ctx* c) {
                     &c->tile_offsets,  &c->image,         &c->tile_costs,    &c->sched_keys_a,
                     &c->sched_keys_b,  &c->sched_order_a, &c->sched_order_b, &c->sched_status,
                     &c->d_views,       &c->ctrl,          &c->model_params,  &c->model_mean,
-                    &c->model_inv_std, &c->tile_feats,    &c->tile_preds};
+                    &c->model_inv_std, &c->tile_feats,    &c->tile_preds,    &c->composite_out};
   for (DevBuf* b : bufs) release(*b);
   for (int i = 0; i < kUploadSlots; ++i)
     if (c->upload_ev[i]) cudaEventDestroy(c->upload_ev[i]);
@@ -802,6 +802,37 @@ int gs3d_add_scene(gs3d_ctx* c, uint32_t n, const float* positions, const float*
     *out_scene = (uint32_t)c->scenes.size() - 1;
   }
   c->have_scene = true;
+  return GS3D_OK;
+}
+
+int gs3d_composite(gs3d_ctx* c, uint32_t view, uint32_t mode, uint32_t debug_ref,
+                   const float background[4], void* rgba8, size_t bytes, int memory) {
+  if (!c || !rgba8) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
+  if (mode > GS3D_COMPOSITE_TILE_HEATMAP)
+    return fail(c, GS3D_ERR_INVALID_ARG, "unknown composite mode %u", mode);
+  if (memory != 0 && memory != 1) return fail(c, GS3D_ERR_INVALID_ARG, "memory must be 0 or 1");
+  if (view >= c->info.size())
+    return fail(c, GS3D_ERR_STATE, "composite: view %u of %zu rendered", view, c->info.size());
+  TRY(set_device(c));
+  const gs3d_view_info& v = c->info[view];
+  const size_t need = (size_t)v.width * v.height * 4;
+  if (bytes < need)
+    return fail(c, GS3D_ERR_INVALID_ARG, "composite needs %zu bytes, got %zu", need, bytes);
+  const float zero[4] = {0.f, 0.f, 0.f, 0.f};
+  uint32_t* dst = static_cast<uint32_t*>(rgba8);
+  if (memory == 0) {
+    TRY(ensure(c, c->composite_out, std::max<size_t>(need, 4), "composite target"));
+    dst = static_cast<uint32_t*>(c->composite_out.p);
+  }
+  CK(launch_composite(static_cast<const uint2*>(c->image.p) + v.pixel_offset, v.width, v.height,
+                      u32(c->tile_offsets) + v.tile_base, c->tile_w, c->tile_h, v.tiles_x,
+                      v.tiles_y, mode, debug_ref ? debug_ref : 256u,
+                      background ? background : zero, dst, c->stream),
+     "composite");
+  if (memory == 0) {
+    CK(cudaMemcpyAsync(rgba8, dst, need, cudaMemcpyDeviceToHost, c->stream), "composite copy");
+    CK(cudaStreamSynchronize(c->stream), "composite copy");
+  }
   return GS3D_OK;
 }
 

@@ -318,6 +318,14 @@ struct RasterArgs {
 };
 cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s);
 
+// Headless composite of one view's splat target over a background colour,
+// optionally through the tile heat-map overlay; out = W*H RGBA8 words.
+cudaError_t launch_composite(const uint2* image, uint32_t W, uint32_t H,
+                             const uint32_t* tile_offsets, uint32_t tile_w, uint32_t tile_h,
+                             uint32_t tiles_x, uint32_t tiles_y, uint32_t heatmap,
+                             uint32_t debug_ref, const float bg[4], uint32_t* out,
+                             cudaStream_t s);
+
 // ---- PLY ingest (ply.cu) ----------------------------------------------------
 enum PlyScalar : uint32_t { PLY_I8, PLY_U8, PLY_I16, PLY_U16, PLY_I32, PLY_U32, PLY_F32, PLY_F64 };
 struct PlyField {

@@ -437,6 +437,27 @@ class GaussianSplatRenderer:
     def readImage(self) -> np.ndarray:
         return self.readBuffer("splat_target")
 
+    def composite(self, view: int = 0, heatmap: bool = False, background=(0.0, 0.0, 0.0, 1.0),
+                  debugRef: int = 256) -> np.ndarray:
+        """The composite pass (and, with heatmap, the splats-per-tile overlay
+        pass before it) rendered headless over a premultiplied background:
+        (H, W, 4) uint8 RGBA."""
+        info = self.viewInfo(view)
+        out = np.zeros((info.height, info.width, 4), np.uint8)
+        bg = np.ascontiguousarray(background, np.float32)
+        self._call("gs3d_composite", int(view),
+                   _lib.COMPOSITE_TILE_HEATMAP if heatmap else _lib.COMPOSITE_SPLATS,
+                   int(debugRef), bg.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p),
+                   out.nbytes, 0)
+        return out
+
+    def saveComposite(self, path, **kw) -> np.ndarray:
+        """composite() written to a PNG file."""
+        from .image import write_png
+        img = self.composite(**kw)
+        write_png(path, img)
+        return img
+
     def readTileCounts(self) -> np.ndarray:
         """readTileCounts (:1278-1310): max(0, off[t+1] - off[t]) per tile."""
         tiles = self.tileCountX * self.tileCountY
