@@ -132,6 +132,28 @@ def algorithmic_bytes(n, R, tiles, tile_passes, sh_floats, fused):
     }
 
 
+# DRAM bytes per unit of the HBM-bound kernels, from ncu captures of a
+# 2-view batch of the same workload (profiles/), scaled to a launch by the
+# units it processes: tile-digit pass per ref (32x32 / 16x16 tiles),
+# preprocess per splat-view, emit per (splat-view, ref).
+DRAM_PER_REF_PASS = {32: 22.6, 16: 25.1}
+DRAM_PREPROCESS_PER_SPLAT = 1894.3e6 / 6e6
+DRAM_EMIT = {32: (1034.6e6, 6e6, 23.7e6), 16: (1484.9e6, 6e6, 57.2e6)}
+
+
+def dominant_traffic(stage, tile, refs_per_launch, splats_per_launch):
+    """Measured DRAM bytes of one launch of the dominant HBM-bound kernel, or
+    None where no capture covers it."""
+    if stage == "radix-sort" and tile in DRAM_PER_REF_PASS:
+        return int(DRAM_PER_REF_PASS[tile] * refs_per_launch)
+    if stage == "preprocess-splats":
+        return int(DRAM_PREPROCESS_PER_SPLAT * splats_per_launch)
+    if stage == "emit-tile-refs" and tile in DRAM_EMIT:
+        b, n, r = DRAM_EMIT[tile]
+        return int(b * (0.5 * splats_per_launch / n + 0.5 * refs_per_launch / r))
+    return None
+
+
 def install_cost_model(lib, ctx, tile):
     """Cost model trained for this tile size, behind its gate; returns the
     schedule to use and the model's held-out metrics (None when no model
@@ -365,6 +387,8 @@ def run_ours(args, rank, world):
         "tuning": {"tile": tuned.tile_w, "digit_bits": tuned.digit_bits,
                    "raster_batch": tuned.raster_batch, "candidates": tune_table},
         "tile_passes_batched": tuned_passes,
+        "traffic": dominant_traffic(dom, tuned.tile_w, tuned_R * B, N_SPLATS * B),
+        "launch_units": {"refs": int(tuned_R * B), "splat_views": N_SPLATS * B},
     }
 
 
@@ -493,7 +517,10 @@ def main():
                        "plain_stagewise_views_per_s": res["stagewise_value"]},
             "roofline": {"bound": "hbm", "kernel": res["dominant"], "achieved": dom["gbs"],
                          "peak": res["peak"], "unit": "GB/s", "frac": dom["frac_hbm"],
-                         "peak_kind": res["peak_kind"], "traffic": None},
+                         "peak_kind": res["peak_kind"], "traffic": res["traffic"],
+                         "traffic_per": "launch (one pass over one batch), ncu DRAM "
+                                        "bytes of a 2-view capture scaled by units",
+                         "launch_units": res["launch_units"]},
             "stages": res["per_stage"],
             "stages_single_view_fused": res["fused_stages"],
             "stages_plain_stagewise": res["stagewise_stages"],
