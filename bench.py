@@ -303,6 +303,13 @@ def run_ours(args, rank, world):
     # headline: batched, autotuned, learned schedule, CUDA graph replays
     batched_ms, _, clocks = timed("batched", batched_schedule, graph=True)
     eager_ms, batched_stages, _ = timed("batched", batched_schedule)  # per-stage events
+    # the raster under each work order on the tuned batched path (same image)
+    sched_batched = {}
+    for name, sc in (("row_major", _lib.SCHEDULE_ROW_MAJOR), ("key_count", _lib.SCHEDULE_KEY_COUNT),
+                     ("learned", batched_schedule)):
+        ms_, st_, _ = timed("batched", sc)
+        sched_batched[name] = {"raster_ms": round(st_["rasterize-tiles"][0], 4),
+                               "views_per_s": round(views * world / (ms_ * 1e-3), 1)}
 
     # ---- e2e: the public batched entry point with host view tables in and
     # pinned host images out, every batch, under the same tuning ----
@@ -382,7 +389,8 @@ def run_ours(args, rank, world):
         "e2e_value": views * world / (e2e_ms * 1e-3), "e2e_wall_value": views / e2e_wall,
         "h2d": 416 * len(cam_structs), "d2h": img_bytes * len(cam_structs),
         "launches_per_step": launches_per_batch * len(batches),
-        "schedules": sched_raster, "learned_active": learned_on,
+        "schedules": sched_raster, "schedules_batched": sched_batched,
+        "learned_active": learned_on,
         "cost_model": {k: round(v, 4) for k, v in (tuned_model or {}).items()},
         "tuning": {"tile": tuned.tile_w, "digit_bits": tuned.digit_bits,
                    "raster_batch": tuned.raster_batch, "candidates": tune_table},
@@ -513,6 +521,7 @@ def main():
                        "raster_schedule": "learned (cost MLP)" if res["learned_active"]
                                           else "key count (cost MLP gated off)",
                        "schedules_single_view": res["schedules"],
+                       "schedules_batched_tuned": res["schedules_batched"],
                        "cost_model_heldout": res["cost_model"],
                        "plain_stagewise_views_per_s": res["stagewise_value"]},
             "roofline": {"bound": "hbm", "kernel": res["dominant"], "achieved": dom["gbs"],

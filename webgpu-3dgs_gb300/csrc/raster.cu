@@ -84,25 +84,42 @@ __device__ __forceinline__ void prepare(SplatStage& s) {
 // rasterize_tiles.wgsl:81-98 for one (pixel, splat) pair, branch-free: a
 // skipped splat contributes alpha = 0, which leaves C and T bit-unchanged.
 // Returns true when the pixel terminates at this splat.
-template <bool EARLY_OUT>
-__device__ __forceinline__ bool blend_one(float pfx, float pfy, const SplatStage& s, Pixel& p,
-                                          bool live) {
+// The splat's alpha at the pixel centre and whether it passes the per-pixel
+// tests (inside the radius, power <= 0, alpha >= 1/255).
+__device__ __forceinline__ float splat_alpha(float pfx, float pfy, const SplatStage& s,
+                                             bool& ok) {
   const float4 a = s.a, b = s.b;
   const float dx = pfx - a.x;
   const float dy = pfy - a.y;
   const float d2 = fmaf(dx, dx, dy * dy);
-  if (EARLY_OUT && !(d2 <= a.z)) return false;  // outside the radius: alpha would be 0
   const float Q = fmaf(b.x * dx, dx, fmaf(b.y * dx, dy, b.z * dy * dy));  // = -power * log2(e)
   const float alpha = fminf(0.99f, a.w * ex2_approx(-Q));
-  const bool ok = live && (d2 <= a.z) && (Q >= 0.0f) && (alpha >= 1.0f / 255.0f);
+  ok = (d2 <= a.z) && (Q >= 0.0f) && (alpha >= 1.0f / 255.0f);
+  return alpha;
+}
+
+// Blends alpha (0 when !ok, which leaves C and T bit-unchanged); returns
+// true when the pixel terminates here.
+__device__ __forceinline__ bool blend_alpha(Pixel& p, const float4 c, float alpha, bool ok) {
   const float al = ok ? alpha : 0.0f;
-  const float4 c = s.c;
   const float ta = p.T * al;
   p.cr = fmaf(ta, c.x, p.cr);
   p.cg = fmaf(ta, c.y, p.cg);
   p.cb = fmaf(ta, c.z, p.cb);
   p.T = p.T * (1.0f - al);
   return ok && p.T < 1.0e-4f;
+}
+
+template <bool EARLY_OUT>
+__device__ __forceinline__ bool blend_one(float pfx, float pfy, const SplatStage& s, Pixel& p,
+                                          bool live) {
+  if (EARLY_OUT) {  // outside the radius: alpha would be 0
+    const float dx = pfx - s.a.x, dy = pfy - s.a.y;
+    if (!(fmaf(dx, dx, dy * dy) <= s.a.z)) return false;
+  }
+  bool ok;
+  const float alpha = splat_alpha(pfx, pfy, s, ok);
+  return blend_alpha(p, s.c, alpha, ok && live);
 }
 
 __device__ __forceinline__ void store_pixel(uint2* image, uint32_t W, uint32_t px, uint32_t py,
@@ -290,11 +307,27 @@ __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, Splat
         const bool hit = j < cnt && rect_may_hit(cur[j], xlo, xhi, ylo, yhi);
         uint32_t mask = __ballot_sync(0xffffffffu, hit);
         while (mask) {
-          const uint32_t b = __ffs(mask) - 1;
+          const uint32_t b0 = __ffs(mask) - 1;
           mask &= mask - 1;
-          if (blend_one<false>(pfx, pfy, cur[k0 + b], p, !done)) {
+          if (mask) {
+            // two hits: both alphas first (independent work for the
+            // scheduler), then the blends in order
+            const uint32_t b1 = __ffs(mask) - 1;
+            mask &= mask - 1;
+            bool ok0, ok1;
+            const float al0 = splat_alpha(pfx, pfy, cur[k0 + b0], ok0);
+            const float al1 = splat_alpha(pfx, pfy, cur[k0 + b1], ok1);
+            if (blend_alpha(p, cur[k0 + b0].c, al0, ok0 && !done)) {
+              done = true;
+              used = bi * D + k0 + b0 + 1;
+            }
+            if (blend_alpha(p, cur[k0 + b1].c, al1, ok1 && !done)) {
+              done = true;
+              used = bi * D + k0 + b1 + 1;
+            }
+          } else if (blend_one<false>(pfx, pfy, cur[k0 + b0], p, !done)) {
             done = true;
-            used = bi * D + k0 + b + 1;
+            used = bi * D + k0 + b0 + 1;
           }
         }
         if (__all_sync(0xffffffffu, done)) break;
