@@ -253,7 +253,8 @@ int gs3d_set_schedule(struct gs3d_ctx* ctx, uint32_t schedule);
  * tile_w x tile_h. */
 typedef struct gs3d_tuning {
     uint32_t tile_w, tile_h;  /* tile pixel size (gs3d_set_tile_size)                 */
-    uint32_t digit_bits;      /* widest radix digit of the tile-id passes: 6 or 8     */
+    uint32_t digit_bits;      /* widest radix digit of the tile-id passes: 4, 6 or 8;
+                                 8 when narrower digits would need over 4 passes     */
     uint32_t raster_batch;    /* splats staged per raster batch: a multiple of 32 in
                                  [32, 1024]; 0 = one per tile pixel                   */
 } gs3d_tuning;
@@ -270,9 +271,10 @@ int gs3d_get_tuning(struct gs3d_ctx* ctx, gs3d_tuning* out);
 
 /* Autotuner: times the batched rebin of `views` (warm-up, then `reps` timed
  * repetitions, CUDA events on the context's stream) under every candidate
- * of tile size {8, 16, 32} square x digit width {6, 8} x raster batch
+ * of tile size {8, 16, 32} square x digit width {4, 6, 8} x raster batch
  * {128, 256, 512}, applies the fastest and writes up to max_results
- * measurements (n_results = candidates measured).  Blocking. */
+ * measurements (n_results = candidates measured; candidates whose refs
+ * exceed the 2^30 limit of one rebin are skipped).  Blocking. */
 int gs3d_autotune(struct gs3d_ctx* ctx, const gs3d_view* views, uint32_t n_views,
                   uint32_t reps, gs3d_tune_result* results, uint32_t max_results,
                   uint32_t* n_results);
@@ -367,6 +369,9 @@ int gs3d_buffer_info(struct gs3d_ctx* ctx, gs3d_buffer which,
 /* Blocking copy-out of the first `bytes` bytes of a named buffer. */
 int gs3d_read_buffer(struct gs3d_ctx* ctx, gs3d_buffer which,
                      void* host_dst, size_t bytes);
+/* Blocking copy-out of bytes [offset, offset + bytes) of a named buffer. */
+int gs3d_read_buffer_range(struct gs3d_ctx* ctx, gs3d_buffer which, size_t offset,
+                           void* host_dst, size_t bytes);
 /* Blocking copy-in (stage-wise parity: feed another implementation's
  * intermediate buffer into the next stage). */
 int gs3d_write_buffer(struct gs3d_ctx* ctx, gs3d_buffer which,

@@ -34,8 +34,8 @@ using namespace gs3d;
 
 namespace {
 
-// Look-back status words carry 30-bit values, which bounds the live count.
-constexpr uint32_t kMaxCapacity = (1u << 30) - 1u;
+// Refs are indexed by u32 and key buffers hold whole 4096-key partitions.
+constexpr uint32_t kMaxCapacity = 0xFFFFE000u;
 constexpr int kUploadSlots = 8;
 constexpr uint32_t kPreBlock = 256;  // preprocess threads per block
 
@@ -246,6 +246,9 @@ int check_device_errors(gs3d_ctx* c) {
   }
   if (e & DEVERR_TIMEOUT)
     return fail(c, GS3D_ERR_TIMEOUT, "a bounded device wait gave up (look-back or bulk copy)");
+  if (e & DEVERR_BUCKET)
+    return fail(c, GS3D_ERR_CAPACITY,
+                "one radix digit of this frame holds 2^30 keys or more; split the batch");
   return fail(c, GS3D_ERR_INVALID_ARG,
               "a sort key's tile id or a splat offset was out of range for this frame");
 }
@@ -383,7 +386,8 @@ int set_views(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views, bool upload
     pixels += (uint64_t)w * h;
     blocks += (sc.n + kPreBlock - 1) / kPreBlock;
   }
-  if (splats > kMaxCapacity) return fail(c, GS3D_ERR_INVALID_ARG, "batch holds too many splats");
+  if (splats >= (1ull << 30))  // depth-sort look-back counts are 30-bit
+    return fail(c, GS3D_ERR_INVALID_ARG, "batch holds 2^30 splat-views or more");
   if (tiles >= (1ull << 31)) return fail(c, GS3D_ERR_INVALID_ARG, "batch holds too many tiles");
   for (ViewDesc& d : vds) {
     d.batch_splats = (uint32_t)splats;
@@ -1097,8 +1101,9 @@ int gs3d_get_view_info(gs3d_ctx* c, uint32_t view, gs3d_view_info* out) {
 
 int gs3d_set_tuning(gs3d_ctx* c, const gs3d_tuning* t) {
   if (!c || !t) return fail(c, GS3D_ERR_INVALID_ARG, "null tuning");
-  if (t->digit_bits != 6 && t->digit_bits != 8)
-    return fail(c, GS3D_ERR_INVALID_ARG, "digit_bits must be 6 or 8 (got %u)", t->digit_bits);
+  if (t->digit_bits != 4 && t->digit_bits != 6 && t->digit_bits != 8)
+    return fail(c, GS3D_ERR_INVALID_ARG, "digit_bits must be 4, 6 or 8 (got %u)",
+                t->digit_bits);
   if (t->raster_batch % 32 != 0 || t->raster_batch > 1024)
     return fail(c, GS3D_ERR_INVALID_ARG,
                 "raster_batch must be 0 or a multiple of 32 up to 1024 (got %u)",
@@ -1138,7 +1143,7 @@ int gs3d_autotune(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views, uint32_
   }
   std::vector<gs3d_tune_result> res;
   int rc = GS3D_OK;
-  const uint32_t tiles[] = {8, 16, 32}, digits[] = {6, 8}, batches[] = {128, 256, 512};
+  const uint32_t tiles[] = {8, 16, 32}, digits[] = {4, 6, 8}, batches[] = {128, 256, 512};
   for (uint32_t tile : tiles) {
     for (uint32_t digit : digits) {
       for (uint32_t batch : batches) {
@@ -1361,6 +1366,23 @@ int gs3d_read_buffer(gs3d_ctx* c, gs3d_buffer which, void* dst, size_t bytes) {
   TRY(set_device(c));
   TRY(sync_and_check(c));
   if (bytes) CK(cudaMemcpy(dst, b->p, bytes, cudaMemcpyDeviceToHost), "copy-out");
+  return GS3D_OK;
+}
+
+int gs3d_read_buffer_range(gs3d_ctx* c, gs3d_buffer which, size_t offset, void* dst,
+                           size_t bytes) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  DevBuf* b = named(c, which);
+  if (!b) return fail(c, GS3D_ERR_INVALID_ARG, "unknown buffer %d", (int)which);
+  if (offset > b->bytes || bytes > b->bytes - offset)
+    return fail(c, GS3D_ERR_INVALID_ARG, "read of [%zu, +%zu) from a %zu-byte buffer", offset,
+                bytes, b->bytes);
+  if (bytes && !dst) return fail(c, GS3D_ERR_INVALID_ARG, "null destination");
+  TRY(set_device(c));
+  TRY(sync_and_check(c));
+  if (bytes)
+    CK(cudaMemcpy(dst, static_cast<const char*>(b->p) + offset, bytes, cudaMemcpyDeviceToHost),
+       "copy-out");
   return GS3D_OK;
 }
 

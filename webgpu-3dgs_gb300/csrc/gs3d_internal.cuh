@@ -68,6 +68,7 @@ enum : uint32_t {
   DEVERR_CAPACITY = 1u,  // live ref count exceeded key capacity: nothing written
   DEVERR_TIMEOUT = 2u,   // a bounded look-back spin gave up
   DEVERR_RANGE = 4u,     // a key's tile id was outside tile_offsets
+  DEVERR_BUCKET = 8u,    // a radix digit held 2^30 keys or more (30-bit look-back counts)
 };
 
 constexpr int kMaxSortPasses = 8;

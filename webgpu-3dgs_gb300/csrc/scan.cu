@@ -10,7 +10,9 @@
 //
 // Status words are 64-bit: [63:34] launch epoch, [33:32] flag, [31:0] value.
 // The epoch changes every launch, so the status array never needs clearing;
-// entries carrying another epoch read as "not ready".
+// entries carrying another epoch read as "not ready".  Prefixes are summed in
+// 64 bits; a total that does not fit 32 bits saturates at 0xffffffff and
+// latches DEVERR_CAPACITY (no rebin can hold that many refs).
 #include "gs3d_internal.cuh"
 
 namespace gs3d {
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t tile_total = __shfl_sync(0xffffffffu, wi, kThreads / 32 - 1);
 
     // ---- decoupled look-back (warp 0) ----
-    uint32_t excl = 0;
+    unsigned long long excl = 0;
     if (tile == 0) {
       if (lane == 0) st_relaxed_u64(status, pack(epoch, kFlagInc, tile_total));
     } else {
@@ -114,25 +116,29 @@ __global__ void __launch_bounds__(kThreads)
         const uint32_t inc_mask = __ballot_sync(0xffffffffu, flag == kFlagInc);
         if (inc_mask) {
           const int first = __ffs(inc_mask) - 1;  // nearest inclusive predecessor
-          uint32_t x = lane <= first ? val : 0u;
+          unsigned long long x = lane <= first ? val : 0u;
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
           excl += x;
           break;
         }
-        uint32_t x = val;
+        unsigned long long x = val;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
         excl += x;
         pred -= 32;
       }
-      if (lane == 0) st_relaxed_u64(status + tile, pack(epoch, kFlagInc, excl + tile_total));
     }
+    const unsigned long long inc = excl + tile_total;
+    const bool overflow = inc > 0xffffffffull;
+    const uint32_t inc32 = overflow ? 0xffffffffu : (uint32_t)inc;
     if (lane == 0) {
-      s_prefix = excl;
+      if (tile > 0) st_relaxed_u64(status + tile, pack(epoch, kFlagInc, inc32));
+      if (overflow) latch_error(err, DEVERR_CAPACITY);
+      s_prefix = overflow ? 0xffffffffu : (uint32_t)excl;
       if (tile == num_tiles - 1) {
-        *total_out = excl + tile_total;
-        out[n] = excl + tile_total;
+        *total_out = inc32;
+        out[n] = inc32;
       }
     }
   }

@@ -235,9 +235,12 @@ __global__ void __launch_bounds__(kPassThreads, 2)
     fence_mbar_init();
   }
   // global bucket bases of this digit place (the scan's barriers also order
-  // the mbarrier initialisation before any wait)
+  // the mbarrier initialisation before any wait).  Look-back counts are kept
+  // modulo 2^30, exact while every bucket holds fewer keys.
   {
-    const uint32_t bb = block_exclusive_256(digit_thread ? __ldg(hist + tid) : 0u, s_wsum);
+    const uint32_t h = digit_thread ? __ldg(hist + tid) : 0u;
+    if (blockIdx.x == 0 && h >= (1u << 30)) latch_error(err, DEVERR_BUCKET);
+    const uint32_t bb = block_exclusive_256(h, s_wsum);
     if (digit_thread) s_bucket[tid] = bb;
   }
   __syncthreads();
@@ -508,7 +511,7 @@ SortPlan make_sort_plan(uint32_t num_tiles, int tile_digit_bits) {
   const int bits = max_tile ? 32 - __builtin_clz(max_tile) : 0;
   // at most kMaxSortPasses - 4 tile passes: wider digits when narrow ones
   // would need more
-  int w = tile_digit_bits == 6 ? 6 : 8;
+  int w = (tile_digit_bits == 4 || tile_digit_bits == 6) ? tile_digit_bits : 8;
   if ((bits + w - 1) / w > kMaxSortPasses - 4) w = 8;
   for (int s = 0; s < bits; s += w) {  // tile-id bits (hi word)
     const int left = bits - s < w ? bits - s : w;  // the top digit may be narrower

@@ -173,7 +173,7 @@ class GaussianSplatRenderer:
     def setTuning(self, tile: int | tuple[int, int] = 16, digit_bits: int = 8,
                   raster_batch: int = 0) -> None:
         """Speed knobs that leave every image bit-identical: square (or
-        (w, h)) tile size, widest tile-id radix digit (6 or 8 bits), splats
+        (w, h)) tile size, widest tile-id radix digit (4, 6 or 8 bits), splats
         staged per raster batch (0 = one per tile pixel)."""
         tw, th = (tile, tile) if isinstance(tile, int) else tile
         t = _lib.Tuning_t(int(tw), int(th), int(digit_bits), int(raster_batch))
@@ -342,20 +342,23 @@ class GaussianSplatRenderer:
         """(keys, values, tile counts) of view v in single-view terms: tile ids
         relative to the view, values as scene splat ids."""
         info = self.viewInfo(v)
-        R = self.refCount()
-        keys = self.readBuffer("sort_keys_a", R)
-        vals = self.readBuffer("sort_values_a", R)
         t0, t1 = info.tile_base, info.tile_base + info.tiles_x * info.tiles_y
-        a, b = np.searchsorted(keys[:, 0], [t0, t1])
-        k = keys[a:b].copy()
-        k[:, 0] -= t0
         total = self._total_tiles()
         off = np.zeros(total + 1, np.uint32)
         self._call("gs3d_read_buffer", _lib.BUFFERS["tile_offsets"],
                    off.ctypes.data_as(C.c_void_p), off.nbytes)
         o = off.astype(np.int64)
-        counts = np.maximum(o[t0 + 1:t1 + 1] - o[t0:t1], 0)
-        return k, vals[a:b] - info.splat_base, counts
+        all_counts = np.maximum(o[1:] - o[:-1], 0)  # exact: trailing tiles hold no refs
+        a = int(all_counts[:t0].sum())
+        b = a + int(all_counts[t0:t1].sum())
+        k = np.zeros((b - a, 2), np.uint32)
+        vals = np.zeros(b - a, np.uint32)
+        self._call("gs3d_read_buffer_range", _lib.BUFFERS["sort_keys_a"], 8 * a,
+                   k.ctypes.data_as(C.c_void_p), k.nbytes)
+        self._call("gs3d_read_buffer_range", _lib.BUFFERS["sort_values_a"], 4 * a,
+                   vals.ctypes.data_as(C.c_void_p), vals.nbytes)
+        k[:, 0] -= t0
+        return k, vals - info.splat_base, all_counts[t0:t1]
 
     def _total_tiles(self) -> int:
         last = self.viewInfo(self._batch - 1)
