@@ -253,7 +253,8 @@ int gs3d_set_schedule(struct gs3d_ctx* ctx, uint32_t schedule);
  * tile_w x tile_h. */
 typedef struct gs3d_tuning {
     uint32_t tile_w, tile_h;  /* tile pixel size (gs3d_set_tile_size)                 */
-    uint32_t digit_bits;      /* widest radix digit of the tile-id passes: 4, 6 or 8;
+    uint32_t digit_bits;      /* widest radix digit of the tile-id passes: 4, 6, 8 or
+                                 11 (fused rebin; the stage-wise sort uses at most 8);
                                  8 when narrower digits would need over 4 passes     */
     uint32_t raster_batch;    /* splats staged per raster batch: a multiple of 32 in
                                  [32, 1024]; 0 = one per tile pixel                   */
@@ -271,7 +272,7 @@ int gs3d_get_tuning(struct gs3d_ctx* ctx, gs3d_tuning* out);
 
 /* Autotuner: times the batched rebin of `views` (warm-up, then `reps` timed
  * repetitions, CUDA events on the context's stream) under every candidate
- * of tile size {8, 16, 32} square x digit width {4, 6, 8} x raster batch
+ * of tile size {8, 16, 32} square x digit width {4, 8, 11} x raster batch
  * {128, 256, 512}, applies the fastest and writes up to max_results
  * measurements (n_results = candidates measured; candidates whose refs
  * exceed the 2^30 limit of one rebin are skipped).  Blocking. */

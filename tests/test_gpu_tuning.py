@@ -37,7 +37,7 @@ def test_every_tuning_renders_the_same_image(renderer):
     renderer.rebinBatch(views)
     want = _images(renderer, views)
     for tile in (8, 16, 32):
-        for digit in (4, 6, 8):
+        for digit in (4, 6, 8, 11):
             for batch in (0, 64, 512):
                 renderer.setTuning(tile, digit, batch)
                 renderer.rebinBatch(views)
@@ -49,7 +49,8 @@ def test_every_tuning_renders_the_same_image(renderer):
 
 
 @pytest.mark.parametrize("tile,digit,batch", [(8, 6, 128), (32, 6, 512), (16, 6, 64),
-                                              (16, 4, 256), (8, 4, 0)])
+                                              (16, 4, 256), (8, 4, 0), (8, 11, 256),
+                                              (16, 11, 0), (32, 11, 512)])
 def test_tuned_keys_match_the_oracle(renderer, oracle, tile, digit, batch):
     """Single-view fused rebin under a non-default tuning: sorted keys,
     values and tile_offsets bit-exact with the oracle's for that tile grid."""
@@ -87,8 +88,8 @@ def test_autotune_applies_the_fastest_candidate(renderer):
     # fewer refs with larger tiles; the 6-bit digit never needs fewer passes
     by = {(r["tile"][0], r["digit_bits"], r["raster_batch"]): r for r in res}
     assert by[(32, 8, 256)]["refs"] < by[(16, 8, 256)]["refs"] < by[(8, 8, 256)]["refs"]
-    assert by[(16, 4, 256)]["tile_passes"] >= by[(16, 6, 256)]["tile_passes"] >= \
-        by[(16, 8, 256)]["tile_passes"]
+    assert by[(16, 4, 256)]["tile_passes"] >= by[(16, 8, 256)]["tile_passes"] >= \
+        by[(16, 11, 256)]["tile_passes"]
     renderer.rebinBatch(views)
     got = _images(renderer, views)
     for v in range(len(views)):
@@ -97,7 +98,7 @@ def test_autotune_applies_the_fastest_candidate(renderer):
 
 
 def test_bad_tunings_are_rejected(renderer):
-    for bad in [(16, 7, 0), (16, 8, 48), (16, 8, 2048), (64, 8, 0)]:
+    for bad in [(16, 7, 0), (16, 12, 0), (16, 8, 48), (16, 8, 2048), (64, 8, 0)]:
         with pytest.raises(Gs3dError) as ei:
             renderer.setTuning(*bad)
         assert ei.value.code == _lib.ERR_INVALID_ARG

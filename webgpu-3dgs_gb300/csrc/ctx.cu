@@ -197,7 +197,7 @@ int ensure_key_capacity(gs3d_ctx* c, uint64_t want) {
   TRY(ensure(c, c->keys_b, alloc * sizeof(uint2), "sort_keys_b"));
   TRY(ensure(c, c->vals_a, alloc * sizeof(uint32_t), "sort_values_a"));
   TRY(ensure(c, c->vals_b, alloc * sizeof(uint32_t), "sort_values_b"));
-  TRY(ensure(c, c->sort_status, sort_status_words(cap, kMaxSortPasses) * sizeof(uint32_t),
+  TRY(ensure(c, c->sort_status, sort_status_words_max(cap) * sizeof(uint32_t),
              "sort look-back status"));
   c->capacity = cap;
   return GS3D_OK;
@@ -565,7 +565,7 @@ int fused_rebin(gs3d_ctx* c) {
                           static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->depth_ids_a),
                           u32(c->sorted_offsets), u32(c->ref_counter), c->capacity,
                           static_cast<uint2*>(c->keys_a.p), u32(c->vals_a), tp,
-                          &k->sort_hist[4][0], &k->error, c->stream),
+                          &k->tile_hist[0][0], &k->error, c->stream),
        "emit (depth order)");
   }
   {
@@ -573,7 +573,7 @@ int fused_rebin(gs3d_ctx* c) {
     CK(launch_sort_tile_passes(tp, u32(c->ref_counter), c->capacity,
                                static_cast<uint2*>(c->keys_a.p), u32(c->vals_a),
                                static_cast<uint2*>(c->keys_b.p), u32(c->vals_b),
-                               u32(c->sort_status), &k->sort_hist[4][0], &k->sort_part_counter[4],
+                               u32(c->sort_status), &k->tile_hist[0][0], &k->sort_part_counter[4],
                                &k->error, c->sm_count, c->stream),
        "tile-digit sort");
   }
@@ -1020,7 +1020,8 @@ int gs3d_radix_sort(gs3d_ctx* c) {
   if (!c) return GS3D_ERR_INVALID_ARG;
   TRY(require_single(c, "radix_sort"));
   TRY(set_device(c));
-  const SortPlan plan = make_sort_plan(c->total_tiles, (int)c->digit_bits);
+  // the stage-wise sort builds 256-bin histograms: digits of at most 8 bits
+  const SortPlan plan = make_sort_plan(c->total_tiles, (int)std::min<uint32_t>(c->digit_bits, 8));
   {
     StageScope t(c, GS3D_STAGE_SORT);
     CK(launch_sort(plan, u32(c->ref_counter), c->capacity, static_cast<uint2*>(c->keys_a.p),
@@ -1101,8 +1102,8 @@ int gs3d_get_view_info(gs3d_ctx* c, uint32_t view, gs3d_view_info* out) {
 
 int gs3d_set_tuning(gs3d_ctx* c, const gs3d_tuning* t) {
   if (!c || !t) return fail(c, GS3D_ERR_INVALID_ARG, "null tuning");
-  if (t->digit_bits != 4 && t->digit_bits != 6 && t->digit_bits != 8)
-    return fail(c, GS3D_ERR_INVALID_ARG, "digit_bits must be 4, 6 or 8 (got %u)",
+  if (t->digit_bits != 4 && t->digit_bits != 6 && t->digit_bits != 8 && t->digit_bits != 11)
+    return fail(c, GS3D_ERR_INVALID_ARG, "digit_bits must be 4, 6, 8 or 11 (got %u)",
                 t->digit_bits);
   if (t->raster_batch % 32 != 0 || t->raster_batch > 1024)
     return fail(c, GS3D_ERR_INVALID_ARG,
@@ -1143,7 +1144,7 @@ int gs3d_autotune(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views, uint32_
   }
   std::vector<gs3d_tune_result> res;
   int rc = GS3D_OK;
-  const uint32_t tiles[] = {8, 16, 32}, digits[] = {4, 6, 8}, batches[] = {128, 256, 512};
+  const uint32_t tiles[] = {8, 16, 32}, digits[] = {4, 8, 11}, batches[] = {128, 256, 512};
   for (uint32_t tile : tiles) {
     for (uint32_t digit : digits) {
       for (uint32_t batch : batches) {

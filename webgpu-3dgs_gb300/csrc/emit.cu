@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(kThreads)
 // g.  Besides the keys/values the kernel accumulates the 256-bin histograms
 // of the tile-id digit places those passes sort, so they need no separate
 // histogram read.
-template <int TP>
+template <int TP, int BINS>
 __global__ void __launch_bounds__(kThreads)
     emit_sorted_kernel(const ViewDesc* __restrict__ views, uint32_t n_views, uint32_t n,
                        const gs3d_projected_splat* __restrict__ proj,
@@ -100,14 +100,14 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ uint32_t s_tminx[kThreads], s_tminy[kThreads], s_w[kThreads], s_cnt[kThreads];
   __shared__ uint32_t s_lo[kThreads], s_id[kThreads], s_tx[kThreads], s_tb[kThreads];
   __shared__ float s_winv[kThreads];
-  __shared__ uint32_t s_hist[TP > 0 ? TP : 1][kRadixBins];
+  __shared__ uint32_t s_hist[TP > 0 ? TP : 1][BINS];
 
   const uint32_t total = *ref_counter;
   if (total > capacity) {
     if (blockIdx.x == 0 && threadIdx.x == 0) latch_error(err, DEVERR_CAPACITY);
     return;
   }
-  for (int k = threadIdx.x; k < TP * kRadixBins; k += kThreads) (&s_hist[0][0])[k] = 0u;
+  for (int k = threadIdx.x; k < TP * BINS; k += kThreads) (&s_hist[0][0])[k] = 0u;
   const uint32_t first = blockIdx.x * kThreads;
   const uint32_t i = first + threadIdx.x;
   if (i < n) {
@@ -168,9 +168,9 @@ __global__ void __launch_bounds__(kThreads)
     for (int p = 0; p < TP; ++p) hist_add_256(s_hist[p], (tile >> sh[p]) & mk[p], live);
   }
   __syncthreads();
-  for (int k = threadIdx.x; k < TP * kRadixBins; k += kThreads) {
+  for (int k = threadIdx.x; k < TP * BINS; k += kThreads) {
     const uint32_t v = (&s_hist[0][0])[k];
-    if (v) atomicAdd(g_hist + k, v);
+    if (v) atomicAdd(g_hist + (k / BINS) * kTileHistStride + k % BINS, v);
   }
 }
 
@@ -192,20 +192,32 @@ cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t
     shp[p] = tile_plan.shift[p];
     mkp[p] = digit_mask(tile_plan.nbits[p]);
   }
-#define GS3D_EMIT_CASE(TP)                                                                     \
+  bool wide = false;  // an 11-bit digit needs 2048-bin histograms
+  for (int p = 0; p < tile_plan.passes; ++p) wide = wide || tile_plan.nbits[p] > 8;
+#define GS3D_EMIT_CASE(TP, BINS)                                                              \
   case TP:                                                                                    \
-    emit_sorted_kernel<TP><<<blocks, kThreads, 0, s>>>(views, n_views, n, proj, sorted_ids,    \
-                                                       sorted_offsets, ref_counter, capacity,  \
-                                                       keys, values, sh, mk, g_hist, err);     \
+    emit_sorted_kernel<TP, BINS><<<blocks, kThreads, 0, s>>>(                                 \
+        views, n_views, n, proj, sorted_ids, sorted_offsets, ref_counter, capacity, keys,     \
+        values, sh, mk, g_hist, err);                                                         \
     break;
-  switch (tile_plan.passes) {
-    GS3D_EMIT_CASE(0)
-    GS3D_EMIT_CASE(1)
-    GS3D_EMIT_CASE(2)
-    GS3D_EMIT_CASE(3)
-    GS3D_EMIT_CASE(4)
-    default:
-      return cudaErrorInvalidValue;
+  if (wide) {
+    switch (tile_plan.passes) {
+      GS3D_EMIT_CASE(1, 2048)
+      GS3D_EMIT_CASE(2, 2048)
+      GS3D_EMIT_CASE(3, 2048)
+      default:
+        return cudaErrorInvalidValue;
+    }
+  } else {
+    switch (tile_plan.passes) {
+      GS3D_EMIT_CASE(0, kRadixBins)
+      GS3D_EMIT_CASE(1, kRadixBins)
+      GS3D_EMIT_CASE(2, kRadixBins)
+      GS3D_EMIT_CASE(3, kRadixBins)
+      GS3D_EMIT_CASE(4, kRadixBins)
+      default:
+        return cudaErrorInvalidValue;
+    }
   }
 #undef GS3D_EMIT_CASE
   return cudaGetLastError();

@@ -73,6 +73,10 @@ enum : uint32_t {
 
 constexpr int kMaxSortPasses = 8;
 constexpr int kRadixBins = 256;
+// Histograms of the fused rebin's tile-id passes: 2048 bins a pass (11-bit
+// digits use them all, narrower digits the first 2^bits).
+constexpr int kTileHistStride = 2048;
+constexpr int kMaxTilePasses = kMaxSortPasses - 4;
 
 // Per-frame control block, zeroed at the start of every rebin.
 struct Ctrl {
@@ -84,6 +88,7 @@ struct Ctrl {
   uint32_t pad[3];
   uint32_t sort_hist[kMaxSortPasses][kRadixBins];  // global digit histograms
   uint32_t sched_hist[2][kRadixBins];
+  uint32_t tile_hist[kMaxTilePasses][kTileHistStride];  // fused rebin's tile passes
 };
 
 // Bounded spins: a device wait gives up after this many polls (with
@@ -202,10 +207,10 @@ struct SortPlan {
   int passes;                    // number of digit passes (digits of up to 8 bits)
   int word[kMaxSortPasses];      // 0 = hi (tile id), 1 = lo (depth bits)
   int shift[kMaxSortPasses];
-  int nbits[kMaxSortPasses];     // digit width of the pass: 2, 4, 6 or 8
+  int nbits[kMaxSortPasses];     // digit width of the pass: 2, 4, 6, 8 or 11
 };
 // 4 depth-bit passes, then the tile-id bits below the highest set bit of
-// num_tiles - 1 in digits of at most tile_digit_bits (6 or 8) bits.  A digit
+// num_tiles - 1 in digits of at most tile_digit_bits (4, 6, 8 or 11) bits.  A digit
 // is (word >> shift) & ((1 << nbits) - 1); digits of neighbouring passes may
 // overlap by a bit, which a stable LSD sequence tolerates.
 SortPlan make_sort_plan(uint32_t num_tiles, int tile_digit_bits = 8);
@@ -236,11 +241,14 @@ cudaError_t launch_sort(const SortPlan& plan, const uint32_t* ref_counter, uint3
                         uint2* keys_a, uint32_t* vals_a, uint2* keys_b, uint32_t* vals_b,
                         uint32_t* status, Ctrl* ctrl, int sm_count, cudaStream_t s);
 size_t sort_status_words(uint32_t capacity, int passes);
+// Status words any sort plan of a capacity needs (11-bit tile passes included).
+size_t sort_status_words_max(uint32_t capacity);
 // Key/value buffers handed to the sort must hold this many entries: passes
 // always fetch whole 4096-key partitions (entries past the live count are
 // read and ignored).
 uint32_t sort_capacity_round(uint32_t capacity);
-// Tile-id passes of the fused rebin: histograms already in g_hist[p][256].
+// Tile-id passes of the fused rebin: histograms already in
+// g_hist[p * kTileHistStride + digit].
 cudaError_t launch_sort_tile_passes(const SortPlan& plan, const uint32_t* ref_counter,
                                     uint32_t capacity, uint2* keys_a, uint32_t* vals_a,
                                     uint2* keys_b, uint32_t* vals_b, uint32_t* status,

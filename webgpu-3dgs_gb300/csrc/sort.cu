@@ -28,6 +28,7 @@
 // (tile id, depth bits, emit position), since every pass is a stable
 // counting sort on one digit.
 #include <algorithm>
+#include <type_traits>
 
 #include "gs3d_internal.cuh"
 
@@ -390,6 +391,273 @@ __global__ void __launch_bounds__(kPassThreads, 2)
   }
 }
 
+// ---- 11-bit digits -----------------------------------------------------------
+// The same pass for 2048-bin digits (tile-id passes of the fused rebin): the
+// per-warp counts take 64 KB, so one CTA runs per SM; every thread owns four
+// consecutive digits for the per-digit work and the look-back.
+constexpr int kWideBits = 11;
+constexpr uint32_t kWideBins = 1u << kWideBits;
+constexpr uint32_t kWideDigitsPerThread = kWideBins / kPassThreads;  // 4
+constexpr int kWideLookback = 8;
+
+template <typename K>
+constexpr size_t wide_pass_smem() {
+  return 2 * part_buf_bytes<K>() + (size_t)kWarps * kWideBins * sizeof(uint16_t) +
+         3 * (size_t)kWideBins * sizeof(uint32_t);
+}
+
+__device__ __forceinline__ uint32_t wide_digit(uint2 k, int word, int shift) {
+  return ((word ? k.y : k.x) >> shift) & (kWideBins - 1u);
+}
+
+// Inclusive scan over lanes 0..15 (the sixteen digit warps' totals).
+__device__ __forceinline__ uint32_t scan16_inclusive(uint32_t x, int lane) {
+#pragma unroll
+  for (int o = 1; o < 16; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+
+__global__ void __launch_bounds__(kPassThreads, 1)
+    onesweep_wide_kernel(const uint2* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                         uint2* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                         const uint32_t* __restrict__ ref_counter, uint32_t capacity, int word,
+                         int shift, const uint32_t* __restrict__ hist,
+                         uint32_t* __restrict__ status, uint32_t* __restrict__ part_counter,
+                         uint32_t* __restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr size_t kBuf = part_buf_bytes<uint2>();
+  uint16_t* s_whist = reinterpret_cast<uint16_t*>(smem + 2 * kBuf);  // [kWarps][2048]
+  uint32_t* s_bucket = reinterpret_cast<uint32_t*>(smem + 2 * kBuf + kWarps * kWideBins * 2);
+  uint32_t* s_dloc = s_bucket + kWideBins;  // exclusive start within the digit warp
+  uint32_t* s_dest = s_dloc + kWideBins;
+  __shared__ uint32_t s_wsum[kWarps];
+  __shared__ uint32_t s_part[2];
+  __shared__ uint64_t s_bar[2];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t R = live_refs(ref_counter, capacity);
+  const uint32_t num_parts = (R + kPart - 1) / kPart;
+  constexpr uint32_t kDigitMask = kWideBins - 1u;
+  const uint32_t d0 = tid * kWideDigitsPerThread;  // this thread's digits d0 .. d0+3
+
+  auto claim_into = [&](int b) {
+    const uint32_t part = atomicAdd(part_counter, 1u);
+    s_part[b] = part;
+    if (part < num_parts) {
+      unsigned char* buf = smem + b * kBuf;
+      const uint32_t kb = kPart * sizeof(uint2), vb = kPart * sizeof(uint32_t);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_expect_tx(&s_bar[b], kb + vb);
+      bulk_g2s(buf, keys_in + (size_t)part * kPart, kb, &s_bar[b]);
+      bulk_g2s(buf + kb, vals_in + (size_t)part * kPart, vb, &s_bar[b]);
+    } else {
+      mbar_arrive(&s_bar[b]);
+    }
+  };
+
+  if (tid == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    fence_mbar_init();
+  }
+  // global bucket bases: exclusive scan of the 2048-bin histogram
+  {
+    uint32_t h[kWideDigitsPerThread], t = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kWideDigitsPerThread; ++k) {
+      h[k] = __ldg(hist + d0 + k);
+      if (blockIdx.x == 0 && h[k] >= (1u << 30)) latch_error(err, DEVERR_BUCKET);
+      t += h[k];
+    }
+    const uint32_t inc = warp_inclusive(t, lane);
+    if (lane == 31) s_wsum[warp] = inc;
+    __syncthreads();
+    const uint32_t wv = lane < kWarps ? s_wsum[lane] : 0u;
+    const uint32_t wex = scan16_inclusive(wv, lane) - wv;
+    uint32_t run = __shfl_sync(0xffffffffu, wex, warp) + inc - t;
+#pragma unroll
+    for (uint32_t k = 0; k < kWideDigitsPerThread; ++k) {
+      s_bucket[d0 + k] = run;
+      run += h[k];
+    }
+  }
+  __syncthreads();
+  if (tid == 0) claim_into(0);
+  int b = 0;
+  uint32_t phase0 = 0, phase1 = 0;
+
+  for (;;) {
+    uint16_t* wh = s_whist + warp * kWideBins;
+#pragma unroll
+    for (int k = 0; k < (int)(kWideBins * 2 / 16 / 32); ++k)  // 4 KB row: 8 x 16 B per lane
+      reinterpret_cast<uint4*>(wh)[lane + 32 * k] = make_uint4(0u, 0u, 0u, 0u);
+    __syncwarp();
+    uint2* s_keys = reinterpret_cast<uint2*>(smem + b * kBuf);
+    uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + b * kBuf + kPart * sizeof(uint2));
+    const bool landed = mbar_wait(&s_bar[b], b ? phase1 : phase0);
+    if (b) phase1 ^= 1u; else phase0 ^= 1u;
+    const uint32_t part = landed ? s_part[b] : num_parts;
+    const uint32_t count = part < num_parts ? min(kPart, R - part * kPart) : 0u;
+
+    uint2 key[kItems];
+    uint32_t val[kItems];
+    uint32_t dr[kItems];  // digit | rank-in-warp << 11
+    const uint32_t wloc = warp * (32u * kItems);
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const uint32_t loc = wloc + i * 32u + lane;
+      if (loc < count) {
+        key[i] = s_keys[loc];
+        val[i] = s_vals[loc];
+      } else {
+        key[i] = make_uint2(0xffffffffu, 0xffffffffu);
+        val[i] = 0u;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const uint32_t d = wide_digit(key[i], word, shift);
+      const uint32_t peers = match_digit<kWideBits>(d);
+      const uint32_t prior = wh[d];
+      __syncwarp();
+      if ((__ffs(peers) - 1) == lane) wh[d] = (uint16_t)(prior + __popc(peers));
+      __syncwarp();
+      dr[i] = d | ((prior + __popc(peers & lanemask_lt())) << kWideBits);
+    }
+    // A: counts complete, input buffer read, the fetch had landed for everyone
+    if (!__syncthreads_and(landed)) {
+      if (tid == 0) {
+        latch_error(err, DEVERR_TIMEOUT);
+        mbar_wait(&s_bar[b], b ? phase1 ^ 1u : phase0 ^ 1u);
+      }
+      break;
+    }
+    if (part >= num_parts) break;
+
+    // ---- per digit: warp offsets, partition totals (four digits a thread) ----
+    uint32_t run[kWideDigitsPerThread], pub[kWideDigitsPerThread];
+    uint32_t t = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kWideDigitsPerThread; ++k) {
+      const uint32_t d = d0 + k;
+      uint32_t r = 0;
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w) {
+        const uint32_t c = s_whist[w * kWideBins + d];
+        s_whist[w * kWideBins + d] = (uint16_t)r;
+        r += c;
+      }
+      run[k] = r;
+      pub[k] = (d == kDigitMask) ? r - (kPart - count) : r;
+      st_relaxed_u32(status + (size_t)part * kWideBins + d,
+                     ((part == 0 ? kFlagInc : kFlagAgg) << 30) | pub[k]);
+      t += r;
+    }
+    {
+      const uint32_t inc = warp_inclusive(t, lane);
+      uint32_t x = inc - t;
+#pragma unroll
+      for (uint32_t k = 0; k < kWideDigitsPerThread; ++k) {
+        s_dloc[d0 + k] = x;  // exclusive within the digit warp (128 digits)
+        x += run[k];
+      }
+      if (lane == 31) s_wsum[warp] = inc;
+    }
+    __syncthreads();  // B
+
+    const uint32_t wv = lane < kWarps ? s_wsum[lane] : 0u;
+    const uint32_t wex = scan16_inclusive(wv, lane) - wv;
+
+    // ---- reorder the partition in place ----
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const uint32_t d = dr[i] & kDigitMask;
+      const uint32_t pos = s_dloc[d] + __shfl_sync(0xffffffffu, wex, d >> 7) + wh[d] +
+                           (dr[i] >> kWideBits);
+      s_keys[pos] = key[i];
+      s_vals[pos] = val[i];
+    }
+
+    // ---- decoupled look-back, four digits a thread ----
+    const uint32_t wbase = __shfl_sync(0xffffffffu, wex, warp);  // digits d0.. are in `warp`
+    uint32_t excl[kWideDigitsPerThread] = {0u, 0u, 0u, 0u};
+    bool ok = true;
+    if (part > 0) {
+      uint32_t found = 0;  // bit k: digit d0 + k reached an inclusive prefix
+      int pp = (int)part - 1;
+      while (found != 0xfu && ok && pp >= 0) {
+        uint32_t lw[kWideLookback][kWideDigitsPerThread];
+#pragma unroll
+        for (int i = 0; i < kWideLookback; ++i)
+#pragma unroll
+          for (uint32_t k = 0; k < kWideDigitsPerThread; ++k)
+            lw[i][k] = (pp - i >= 0 && !((found >> k) & 1u))
+                           ? ld_relaxed_u32(status + (size_t)(pp - i) * kWideBins + d0 + k)
+                           : (kFlagInc << 30);
+#pragma unroll
+        for (uint32_t k = 0; k < kWideDigitsPerThread; ++k) {
+#pragma unroll
+          for (int i = 0; i < kWideLookback; ++i) {
+            if (((found >> k) & 1u) || !ok) break;
+            uint32_t spins = 0;
+            while ((lw[i][k] >> 30) == 0u) {  // not published yet: poll this one
+              if (++spins > kSpinLimit) {
+                ok = false;
+                break;
+              }
+              if (spins > 16) __nanosleep(32);
+              lw[i][k] = ld_relaxed_u32(status + (size_t)(pp - i) * kWideBins + d0 + k);
+            }
+            if (!ok) break;
+            if (pp - i >= 0) excl[k] += lw[i][k] & kValueMask;
+            if ((lw[i][k] >> 30) == kFlagInc) found |= 1u << k;
+          }
+        }
+        pp -= kWideLookback;
+      }
+#pragma unroll
+      for (uint32_t k = 0; k < kWideDigitsPerThread; ++k)
+        st_relaxed_u32(status + (size_t)part * kWideBins + d0 + k,
+                       (kFlagInc << 30) | ((excl[k] + pub[k]) & kValueMask));
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kWideDigitsPerThread; ++k)
+      s_dest[d0 + k] = s_bucket[d0 + k] + excl[k] - (s_dloc[d0 + k] + wbase);
+    // C: partition reordered, destinations resolved
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0) latch_error(err, DEVERR_TIMEOUT);
+      break;
+    }
+    if (tid == kPassThreads - 1) claim_into(b ^ 1);
+    for (uint32_t j = tid; j < count; j += kPassThreads) {
+      const uint2 k = s_keys[j];
+      const uint32_t dst = s_dest[wide_digit(k, word, shift)] + j;
+      if (dst < R) {
+        keys_out[dst] = k;
+        vals_out[dst] = s_vals[j];
+      } else {
+        latch_error(err, DEVERR_RANGE);
+      }
+    }
+    b ^= 1;
+  }
+}
+
+cudaError_t onesweep_wide_setup() {
+  static bool done = false;  // per process: the library drives one device
+  if (!done) {
+    cudaError_t e = cudaFuncSetAttribute(onesweep_wide_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)wide_pass_smem<uint2>());
+    if (e != cudaSuccess) return e;
+    done = true;
+  }
+  return cudaSuccess;
+}
+
 template <typename K, int NBITS>
 cudaError_t onesweep_setup(int* per_sm) {
   static int v = 0;  // per process: the library drives one device
@@ -425,6 +693,19 @@ cudaError_t launch_pass(int nbits, const K* kin, const uint32_t* vin, K* kout, u
                                                               shift, hist, status,           \
                                                               part_counter, err);            \
   break;
+  if (nbits == kWideBits) {  // 2048-bin digits: (tile | depth) keys only
+    if constexpr (std::is_same<K, uint2>::value) {
+      e = onesweep_wide_setup();
+      if (e != cudaSuccess) return e;
+      onesweep_wide_kernel<<<(int)std::min<size_t>((size_t)sm_count, parts_cap), kPassThreads,
+                             wide_pass_smem<uint2>(), s>>>(kin, vin, kout, vout, ref_counter,
+                                                           capacity, word, shift, hist, status,
+                                                           part_counter, err);
+      return cudaGetLastError();
+    } else {
+      return cudaErrorInvalidValue;
+    }
+  }
   switch (nbits) {  // 2, 4, 6 or 8 (make_sort_plan)
     case 2: GS3D_PASS(2)
     case 4: GS3D_PASS(4)
@@ -466,11 +747,20 @@ cudaError_t launch_histogram(int passes, const PassDev& pd, const K* keys,
 template <typename K>
 cudaError_t run_passes(const SortPlan& plan, const uint32_t* ref_counter, uint32_t capacity,
                        K* keys_a, uint32_t* vals_a, K* keys_b, uint32_t* vals_b,
-                       uint32_t* status, uint32_t* g_hist, uint32_t* part_counters,
-                       uint32_t* err, bool hist_ready, int sm_count, cudaStream_t s) {
+                       uint32_t* status, uint32_t* g_hist, size_t hist_stride,
+                       uint32_t* part_counters, uint32_t* err, bool hist_ready, int sm_count,
+                       cudaStream_t s) {
   cudaError_t e = cudaSuccess;
   const size_t parts_cap = ((size_t)capacity + kPart - 1) / kPart + 1;
   const size_t stride = parts_cap * kRadixBins;
+  // look-back status of pass p: parts_cap words per bin, passes back to back
+  size_t status_off[kMaxSortPasses + 1] = {0};
+  for (int p = 0; p < plan.passes; ++p)
+    status_off[p + 1] =
+        status_off[p] + parts_cap * (plan.nbits[p] == kWideBits ? kWideBins : kRadixBins);
+  if (!hist_ready)  // the histogram kernel builds 256-bin histograms only
+    for (int p = 0; p < plan.passes; ++p)
+      if (plan.nbits[p] > 8 || hist_stride != kRadixBins) return cudaErrorInvalidValue;
   PassDev pd{};
   for (int p = 0; p < plan.passes; ++p) {
     pd.word[p] = plan.word[p];
@@ -481,16 +771,15 @@ cudaError_t run_passes(const SortPlan& plan, const uint32_t* ref_counter, uint32
     e = launch_histogram<K>(plan.passes, pd, keys_a, ref_counter, capacity, g_hist, status,
                             stride, sm_count * 4, s);
   } else {
-    e = cudaMemsetAsync(status, 0, stride * plan.passes * sizeof(uint32_t), s);
+    e = cudaMemsetAsync(status, 0, status_off[plan.passes] * sizeof(uint32_t), s);
   }
   if (e != cudaSuccess) return e;
   for (int p = 0; p < plan.passes; ++p) {
     const bool even = (p % 2) == 0;
     e = launch_pass<K>(plan.nbits[p], even ? keys_a : keys_b, even ? vals_a : vals_b,
                        even ? keys_b : keys_a, even ? vals_b : vals_a, ref_counter, capacity,
-                       plan.word[p], plan.shift[p], g_hist + (size_t)p * kRadixBins,
-                       status + (size_t)p * stride, part_counters + p, err, sm_count, parts_cap,
-                       s);
+                       plan.word[p], plan.shift[p], g_hist + (size_t)p * hist_stride,
+                       status + status_off[p], part_counters + p, err, sm_count, parts_cap, s);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -511,13 +800,15 @@ SortPlan make_sort_plan(uint32_t num_tiles, int tile_digit_bits) {
   const int bits = max_tile ? 32 - __builtin_clz(max_tile) : 0;
   // at most kMaxSortPasses - 4 tile passes: wider digits when narrow ones
   // would need more
-  int w = (tile_digit_bits == 4 || tile_digit_bits == 6) ? tile_digit_bits : 8;
+  int w = (tile_digit_bits == 4 || tile_digit_bits == 6 || tile_digit_bits == 11)
+              ? tile_digit_bits : 8;
   if ((bits + w - 1) / w > kMaxSortPasses - 4) w = 8;
   for (int s = 0; s < bits; s += w) {  // tile-id bits (hi word)
     const int left = bits - s < w ? bits - s : w;  // the top digit may be narrower
     p.word[n] = 0;
     p.shift[n] = s;
-    p.nbits[n] = (left + 1) & ~1;  // kernels exist for 2, 4, 6 and 8 bits
+    // kernels exist for 2, 4, 6, 8 and 11 bits
+    p.nbits[n] = left > 8 ? kWideBits : (left + 1) & ~1;
     ++n;
   }
   p.passes = n;
@@ -533,6 +824,12 @@ size_t sort_status_words(uint32_t capacity, int passes) {
   return parts * kRadixBins * (size_t)passes;
 }
 
+size_t sort_status_words_max(uint32_t capacity) {
+  // the larger of 8 passes of 256 bins and 4 tile passes, 3 of them 2048-bin
+  const size_t parts = ((size_t)capacity + kPart - 1) / kPart + 1;
+  return parts * std::max<size_t>(kMaxSortPasses * kRadixBins, 3 * kWideBins + kRadixBins);
+}
+
 cudaError_t launch_sort(const SortPlan& plan, const uint32_t* ref_counter, uint32_t capacity,
                         uint2* keys_a, uint32_t* vals_a, uint2* keys_b, uint32_t* vals_b,
                         uint32_t* status, Ctrl* ctrl, int sm_count, cudaStream_t s) {
@@ -542,8 +839,8 @@ cudaError_t launch_sort(const SortPlan& plan, const uint32_t* ref_counter, uint3
                                   s);
   if (e != cudaSuccess) return e;
   return run_passes<uint2>(plan, ref_counter, capacity, keys_a, vals_a, keys_b, vals_b, status,
-                           &ctrl->sort_hist[0][0], ctrl->sort_part_counter, &ctrl->error,
-                           false, sm_count, s);
+                           &ctrl->sort_hist[0][0], kRadixBins, ctrl->sort_part_counter,
+                           &ctrl->error, false, sm_count, s);
 }
 
 cudaError_t launch_sort_tile_passes(const SortPlan& plan, const uint32_t* ref_counter,
@@ -552,7 +849,7 @@ cudaError_t launch_sort_tile_passes(const SortPlan& plan, const uint32_t* ref_co
                                     uint32_t* g_hist, uint32_t* part_counters, uint32_t* err,
                                     int sm_count, cudaStream_t s) {
   return run_passes<uint2>(plan, ref_counter, capacity, keys_a, vals_a, keys_b, vals_b, status,
-                           g_hist, part_counters, err, true, sm_count, s);
+                           g_hist, kTileHistStride, part_counters, err, true, sm_count, s);
 }
 
 cudaError_t launch_sort_u32(const SortPlan& plan, const uint32_t* count, uint32_t capacity,
@@ -560,7 +857,7 @@ cudaError_t launch_sort_u32(const SortPlan& plan, const uint32_t* count, uint32_
                             uint32_t* vals_b, uint32_t* status, uint32_t* g_hist,
                             uint32_t* part_counters, uint32_t* err, int sm_count, cudaStream_t s) {
   return run_passes<uint32_t>(plan, count, capacity, keys_a, vals_a, keys_b, vals_b, status,
-                              g_hist, part_counters, err, false, sm_count, s);
+                              g_hist, kRadixBins, part_counters, err, false, sm_count, s);
 }
 
 cudaError_t launch_sort_depth_keys(const uint32_t* count, uint32_t capacity, uint32_t* keys_a,
@@ -575,7 +872,7 @@ cudaError_t launch_sort_depth_keys(const uint32_t* count, uint32_t capacity, uin
     plan.nbits[p] = 8;
   }
   return run_passes<uint32_t>(plan, count, capacity, keys_a, vals_a, keys_b, vals_b, status,
-                              g_hist, part_counters, err, false, sm_count, s);
+                              g_hist, kRadixBins, part_counters, err, false, sm_count, s);
 }
 
 }  // namespace gs3d

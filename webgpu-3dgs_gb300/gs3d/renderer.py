@@ -173,7 +173,7 @@ class GaussianSplatRenderer:
     def setTuning(self, tile: int | tuple[int, int] = 16, digit_bits: int = 8,
                   raster_batch: int = 0) -> None:
         """Speed knobs that leave every image bit-identical: square (or
-        (w, h)) tile size, widest tile-id radix digit (4, 6 or 8 bits), splats
+        (w, h)) tile size, widest tile-id radix digit (4, 6, 8 or 11 bits), splats
         staged per raster batch (0 = one per tile pixel)."""
         tw, th = (tile, tile) if isinstance(tile, int) else tile
         t = _lib.Tuning_t(int(tw), int(th), int(digit_bits), int(raster_batch))
