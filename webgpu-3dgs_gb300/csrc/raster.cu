@@ -345,9 +345,98 @@ __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, Splat
   }
 }
 
+// Culled variant with two pixels a thread: each warp owns an 8x8 block,
+// lane (x, y) shading rows y and y + 4, so a staged splat is loaded, culled
+// and looped over once for 64 pixels.  blockDim.x == tile_w * tile_h / 2;
+// tile sides divide by 8.  Per pixel the arithmetic and the splat sequence
+// are those of the other variants (bit-identical image).
+__device__ void raster_tile_culled2(const RasterArgs& a, const TileGeom& g, SplatStage* buf0,
+                                    SplatStage* buf1, uint32_t* s_cost) {
+  const uint32_t nt = a.tile_w * a.tile_h;
+  const uint32_t nthr = nt / 2;
+  const uint32_t D = a.batch ? a.batch : nt;  // splats per staged batch
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t bw = a.tile_w / 8;
+  const uint32_t px = g.ox + (warp % bw) * 8 + (lane & 7);
+  const uint32_t py0 = g.oy + (warp / bw) * 8 + (lane >> 3), py1 = py0 + 4;
+  const bool in0 = px < g.W && py0 < g.H, in1 = px < g.W && py1 < g.H;
+  const float pfx = (float)px + 0.5f, pfy0 = (float)py0 + 0.5f, pfy1 = (float)py1 + 0.5f;
+  float xlo = pfx, xhi = pfx, ylo = pfy0, yhi = pfy1;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    xlo = fminf(xlo, __shfl_xor_sync(0xffffffffu, xlo, o));
+    xhi = fmaxf(xhi, __shfl_xor_sync(0xffffffffu, xhi, o));
+    ylo = fminf(ylo, __shfl_xor_sync(0xffffffffu, ylo, o));
+    yhi = fmaxf(yhi, __shfl_xor_sync(0xffffffffu, yhi, o));
+  }
+
+  const uint32_t start = __ldg(a.tile_offsets + g.tile);
+  const uint32_t end = __ldg(a.tile_offsets + g.tile + 1);
+  const uint32_t len = end > start ? end - start : 0u;
+  const uint32_t nbatches = (len + D - 1) / D;
+
+  Pixel p0{0.f, 0.f, 0.f, 1.0f}, p1{0.f, 0.f, 0.f, 1.0f};
+  bool done0 = !in0, done1 = !in1;
+  uint32_t used0 = 0, used1 = 0;
+
+  if (nbatches > 0) stage_batch(a.proj, a.values, start, end, D, nthr, buf0);
+  for (uint32_t bi = 0; bi < nbatches; ++bi) {
+    SplatStage* cur = (bi & 1) ? buf1 : buf0;
+    if (bi + 1 < nbatches) {
+      stage_batch(a.proj, a.values, start + (bi + 1) * D, end, D, nthr, (bi & 1) ? buf0 : buf1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    const uint32_t cnt = min(D, end - (start + bi * D));
+    for (uint32_t k = tid; k < cnt; k += nthr) prepare(cur[k]);  // own copies are complete
+    __syncthreads();
+    if (__any_sync(0xffffffffu, !(done0 && done1))) {
+      for (uint32_t k0 = 0; k0 < cnt; k0 += 32) {
+        const uint32_t j = k0 + lane;
+        const bool hit = j < cnt && rect_may_hit(cur[j], xlo, xhi, ylo, yhi);
+        uint32_t mask = __ballot_sync(0xffffffffu, hit);
+        while (mask) {
+          const uint32_t b = __ffs(mask) - 1;
+          mask &= mask - 1;
+          const SplatStage& sp = cur[k0 + b];
+          bool ok0, ok1;
+          const float al0 = splat_alpha(pfx, pfy0, sp, ok0);
+          const float al1 = splat_alpha(pfx, pfy1, sp, ok1);
+          if (blend_alpha(p0, sp.c, al0, ok0 && !done0)) {
+            done0 = true;
+            used0 = bi * D + k0 + b + 1;
+          }
+          if (blend_alpha(p1, sp.c, al1, ok1 && !done1)) {
+            done1 = true;
+            used1 = bi * D + k0 + b + 1;
+          }
+        }
+        if (__all_sync(0xffffffffu, done0 && done1)) break;
+      }
+      if (!done0) used0 = bi * D + cnt;
+      if (!done1) used1 = bi * D + cnt;
+    }
+    if (__syncthreads_and(done0 && done1)) {
+      cp_async_wait<0>();
+      break;
+    }
+  }
+  if (in0) {
+    atomicMax(s_cost, used0);
+    store_pixel(g.image, g.W, px, py0, p0);
+  }
+  if (in1) {
+    atomicMax(s_cost, used1);
+    store_pixel(g.image, g.W, px, py1, p1);
+  }
+}
+
 // Persistent CTAs pull tile indices from the work queue.
-template <bool CULLED>
-__global__ void raster_kernel(RasterArgs a) {
+// Persistent CTAs over the queue; MODE 0: one thread per pixel, linear;
+// 1: culled, 8x4 warp blocks; 2: culled, two pixels a thread, 8x8 blocks.
+template <int MODE>
+__device__ __forceinline__ void raster_loop(const RasterArgs& a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const uint32_t D = a.batch ? a.batch : a.tile_w * a.tile_h;
   SplatStage* buf0 = reinterpret_cast<SplatStage*>(smem);
@@ -363,13 +452,22 @@ __global__ void raster_kernel(RasterArgs a) {
     if (item >= a.num_tiles) break;
     const uint32_t t = a.order != nullptr ? __ldg(a.order + item) : item;
     const TileGeom g = tile_geom(a, t);
-    if (CULLED)
+    if (MODE == 2)
+      raster_tile_culled2(a, g, buf0, buf1, &s_cost);
+    else if (MODE == 1)
       raster_tile_culled(a, g, buf0, buf1, &s_cost);
     else
       raster_tile_plain(a, g, buf0, buf1, &s_cost);
     __syncthreads();  // s_cost complete; shared buffers free for the next tile
     if (threadIdx.x == 0 && a.tile_costs != nullptr) a.tile_costs[t] = s_cost;
   }
+}
+
+__global__ void raster_kernel_plain(RasterArgs a) { raster_loop<0>(a); }
+__global__ void raster_kernel_culled(RasterArgs a) { raster_loop<1>(a); }
+// 512 threads (a 32x32 tile), two CTAs per SM
+__global__ void __launch_bounds__(512, 2) raster_kernel_culled2(RasterArgs a) {
+  raster_loop<2>(a);
 }
 
 }  // namespace
@@ -380,12 +478,17 @@ cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s) {
   if (a.batch % 32 != 0 || a.batch > 1024) return cudaErrorInvalidValue;
   const uint32_t D = a.batch ? a.batch : nt;
   const bool culled = a.culled && (nt % 32 == 0);
+  // two pixels a thread where the tile splits into 8x8 blocks and at least
+  // 512 pixels
+  const int mode = !culled ? 0 : (a.tile_w % 8 == 0 && a.tile_h % 8 == 0 && nt >= 512) ? 2 : 1;
+  const uint32_t threads = mode == 2 ? nt / 2 : nt;
   const size_t smem = 2 * (size_t)D * sizeof(SplatStage);
-  auto kern = culled ? raster_kernel<true> : raster_kernel<false>;
+  auto kern = mode == 2 ? raster_kernel_culled2 : mode == 1 ? raster_kernel_culled
+                                                             : raster_kernel_plain;
   // launch configuration per (variant, tile area, batch), computed once per process
   static std::mutex mu;
   static std::map<uint64_t, int> cache;
-  const uint64_t key = ((uint64_t)(culled ? 1 : 0) << 40) | ((uint64_t)nt << 20) | D;
+  const uint64_t key = ((uint64_t)mode << 40) | ((uint64_t)nt << 20) | D;
   int per_sm = 0;
   {
     std::lock_guard<std::mutex> lock(mu);
@@ -399,7 +502,7 @@ cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s) {
                                          (int)(2 * 1024 * sizeof(SplatStage)));
     if (e != cudaSuccess) return e;
     int n = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, (int)nt, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, (int)threads, smem);
     if (e != cudaSuccess) return e;
     per_sm = std::max(n, 1);
     std::lock_guard<std::mutex> lock(mu);
@@ -407,7 +510,7 @@ cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s) {
   }
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
       a.num_tiles, (uint64_t)sm_count * (uint64_t)std::max(per_sm, 1));
-  kern<<<grid, nt, smem, s>>>(a);
+  kern<<<grid, threads, smem, s>>>(a);
   return cudaGetLastError();
 }
 
