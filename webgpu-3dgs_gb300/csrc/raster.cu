@@ -465,7 +465,7 @@ __device__ __forceinline__ void raster_loop(const RasterArgs& a) {
 
 __global__ void raster_kernel_plain(RasterArgs a) { raster_loop<0>(a); }
 __global__ void raster_kernel_culled(RasterArgs a) { raster_loop<1>(a); }
-// 512 threads (a 32x32 tile), two CTAs per SM
+// at most 512 threads (a 32x32 tile), two such CTAs per SM
 __global__ void __launch_bounds__(512, 2) raster_kernel_culled2(RasterArgs a) {
   raster_loop<2>(a);
 }
@@ -478,9 +478,8 @@ cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s) {
   if (a.batch % 32 != 0 || a.batch > 1024) return cudaErrorInvalidValue;
   const uint32_t D = a.batch ? a.batch : nt;
   const bool culled = a.culled && (nt % 32 == 0);
-  // two pixels a thread where the tile splits into 8x8 blocks and at least
-  // 512 pixels
-  const int mode = !culled ? 0 : (a.tile_w % 8 == 0 && a.tile_h % 8 == 0 && nt >= 512) ? 2 : 1;
+  // two pixels a thread where the tile splits into 8x8 blocks
+  const int mode = !culled ? 0 : (a.tile_w % 8 == 0 && a.tile_h % 8 == 0) ? 2 : 1;
   const uint32_t threads = mode == 2 ? nt / 2 : nt;
   const size_t smem = 2 * (size_t)D * sizeof(SplatStage);
   auto kern = mode == 2 ? raster_kernel_culled2 : mode == 1 ? raster_kernel_culled
