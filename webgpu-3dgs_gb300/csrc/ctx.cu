@@ -368,7 +368,6 @@ int set_views(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views, bool upload
     d.sh = sc.sh_degree ? static_cast<const float*>(sc.sh.p) : nullptr;
     d.sh_degree = sc.sh_degree;
     d.splat_base = (uint32_t)splats;
-    d.block_base = (uint32_t)blocks;
     d.pixel_base = pixels;
     gs3d_view_info& vi = infos[v];
     vi.pixel_offset = pixels;
@@ -381,10 +380,25 @@ int set_views(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views, bool upload
     vi.splat_count = sc.n;
     vi.scene = in.scene;
     max_sh = std::max(max_sh, d.sh ? sc.sh_degree : 0u);
+    d.group_next = kNoView;
     splats += sc.n;
     tiles += (uint64_t)tx * ty;
     pixels += (uint64_t)w * h;
-    blocks += (sc.n + kPreBlock - 1) / kPreBlock;
+  }
+  // scene groups: views of one scene are projected by one preprocess block
+  // per 256 splats (the first view of the scene leads, the others chain)
+  {
+    std::vector<int64_t> last(c->scenes.size(), -1);
+    for (uint32_t v = 0; v < n_views; ++v) {
+      const uint32_t sid = views[v].scene;
+      vds[v].block_base = (uint32_t)blocks;
+      if (last[sid] < 0) {
+        blocks += (c->scenes[sid].n + kPreBlock - 1) / kPreBlock;
+      } else {
+        vds[(size_t)last[sid]].group_next = v;
+      }
+      last[sid] = v;
+    }
   }
   if (splats >= (1ull << 30))  // depth-sort look-back counts are 30-bit
     return fail(c, GS3D_ERR_INVALID_ARG, "batch holds 2^30 splat-views or more");

@@ -43,13 +43,14 @@ struct ViewDesc {
   const float* sh;
   uint32_t sh_degree;
   uint32_t splat_base;
-  uint32_t block_base;  // first preprocess block of this view
+  uint32_t block_base;  // preprocess blocks of the scene groups' leaders before this view
   uint32_t batch_splats;  // splat-views in the whole batch (same in every view)
   uint64_t pixel_base;  // first pixel of this view's image in the batch target
   uint32_t batch_tiles;   // tiles in the whole batch (same in every view)
-  uint32_t pad1;
+  uint32_t group_next;    // next view of the same scene in the batch, or kNoView
   uint64_t pad2;
 };
+constexpr uint32_t kNoView = 0xffffffffu;
 static_assert(sizeof(ViewDesc) % 16 == 0, "ViewDesc is copied as 16-byte words");
 
 // Largest v with key(v) <= x over a non-decreasing per-view field.

@@ -1,9 +1,12 @@
 // preprocess.cu - stage 1 of the rebin: EWA projection of every splat.
 //
 // Follows src/shaders/compute/preprocess_splats.wgsl:76-184.  One thread per
-// splat; the four vec4 splat arrays are read with 128-bit coalesced loads and
-// the per-block slice of the SH coefficients (extension, SH degree 1..3) is
-// staged into shared memory by one bulk (TMA) copy completing on an mbarrier.
+// splat of a scene; the four vec4 splat arrays are read with 128-bit
+// coalesced loads and the per-block slice of the SH coefficients (extension,
+// SH degree 1..3) is staged into shared memory by one bulk (TMA) copy
+// completing on an mbarrier.  In a batch every view of the same scene is
+// projected by the same thread, so the splat data leaves HBM once per batch,
+// not once per view.
 //
 // Numerics: this translation unit is compiled with -fmad=false and IEEE
 // division / square root, and every expression below is written in the same
@@ -72,9 +75,13 @@ __device__ __forceinline__ void sh_color(float px, float py, float pz, const flo
   }
 }
 
-// preprocess_splats.wgsl:76-184 for the block's 256 splats of one view.
+// preprocess_splats.wgsl:76-184 for the block's 256 splats of one scene, for
+// every view of the batch that renders the scene (the chain leader ->
+// group_next): the splat arrays, the SH slice and the 3D covariance are read
+// and built once, the projection runs per view.
 template <int DEG>
-__device__ __forceinline__ void preprocess_block(const ViewDesc& vd, uint32_t local_first,
+__device__ __forceinline__ void preprocess_block(const ViewDesc* __restrict__ views,
+                                                 uint32_t leader, uint32_t local_first,
                                                  float* s_sh, uint64_t* s_bar,
                                                  gs3d_projected_splat* __restrict__ out,
                                                  uint32_t* __restrict__ counts,
@@ -83,18 +90,17 @@ __device__ __forceinline__ void preprocess_block(const ViewDesc& vd, uint32_t lo
                                                  uint32_t* __restrict__ err) {
   constexpr int K = (DEG + 1) * (DEG + 1) - 1;
   constexpr int KC = 3 * K;  // floats of SH rest per splat
-  const FrameUniforms* fu = &vd.f;
-  const uint32_t n = vd.f.splat_count;
+  const ViewDesc& lv = views[leader];
+  const uint32_t n = lv.f.splat_count;
   const uint32_t li = local_first + threadIdx.x;
   const bool active = li < n;
-  const uint32_t gi = vd.splat_base + li;  // global splat-view index
 
   // ---- SH slice: one bulk copy per block (issued first, waited on late) ----
   bool bulk = false;
   if (DEG > 0) {
     const uint32_t cnt = min((uint32_t)kThreads, n - local_first);
     const uint32_t bytes = cnt * KC * 4u;
-    const float* src = vd.sh + (size_t)local_first * KC;
+    const float* src = lv.sh + (size_t)local_first * KC;
     bulk = (bytes % 16u) == 0u && (reinterpret_cast<uintptr_t>(src) % 16u) == 0u;
     if (bulk) {
       if (threadIdx.x == 0) {
@@ -112,154 +118,163 @@ __device__ __forceinline__ void preprocess_block(const ViewDesc& vd, uint32_t lo
     }
   }
 
-  const float* V = fu->cam.view;
-  const float* P = fu->cam.projection;
-
-  bool valid = false;
-  float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
-  uint4 r3 = make_uint4(0u, 0u, 0u, 0u);
-  uint32_t count = 0;
-  float4 p = r0, col = r0;
-
+  // ---- view-independent: the splat and its 3D covariance S = M M^T ----
+  float4 p = make_float4(0.f, 0.f, 0.f, 0.f), col = p;
+  float S[3][3] = {};
   if (active) {
-    p = __ldg(vd.pos + li);
-    const float4 s = __ldg(vd.scale + li);
-    const float4 q = __ldg(vd.rot + li);
-    col = __ldg(vd.color + li);
+    p = __ldg(lv.pos + li);
+    const float4 s = __ldg(lv.scale + li);
+    const float4 q = __ldg(lv.rot + li);
+    col = __ldg(lv.color + li);
+    const float qw = q.x, qx = q.y, qy = q.z, qz = q.w;
+    const float xx = qx * qx, yy = qy * qy, zz = qz * qz;
+    const float xy = qx * qy, xz = qx * qz, yz = qy * qz;
+    const float wx = qw * qx, wy = qw * qy, wz = qw * qz;
+    float R[3][3];  // [col][row]
+    R[0][0] = 1.0f - 2.0f * (yy + zz); R[0][1] = 2.0f * (xy + wz);        R[0][2] = 2.0f * (xz - wy);
+    R[1][0] = 2.0f * (xy - wz);        R[1][1] = 1.0f - 2.0f * (xx + zz); R[1][2] = 2.0f * (yz + wx);
+    R[2][0] = 2.0f * (xz + wy);        R[2][1] = 2.0f * (yz - wx);        R[2][2] = 1.0f - 2.0f * (xx + yy);
+    const float sc[3] = {s.x, s.y, s.z};
+    float M[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int r = 0; r < 3; ++r) M[k][r] = R[k][r] * sc[k];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+        S[a][b] = M[0][a] * M[0][b] + M[1][a] * M[1][b] + M[2][a] * M[2][b];
+  }
+  bool sh_ready = true;
+  if (DEG > 0 && bulk && !mbar_wait(s_bar, 0)) {
+    if (threadIdx.x == 0) latch_error(err, DEVERR_TIMEOUT);
+    sh_ready = false;
+  }
 
-    float vp[4], cp[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-      vp[r] = __ldg(V + 0 * 4 + r) * p.x + __ldg(V + 1 * 4 + r) * p.y +
-              __ldg(V + 2 * 4 + r) * p.z + __ldg(V + 3 * 4 + r) * 1.0f;
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-      cp[r] = __ldg(P + 0 * 4 + r) * vp[0] + __ldg(P + 1 * 4 + r) * vp[1] +
-              __ldg(P + 2 * 4 + r) * vp[2] + __ldg(P + 3 * 4 + r) * vp[3];
+  for (uint32_t v = leader; v != kNoView; v = views[v].group_next) {
+    const ViewDesc& vd = views[v];
+    const FrameUniforms* fu = &vd.f;
+    const uint32_t gi = vd.splat_base + li;  // global splat-view index
+    const float* V = fu->cam.view;
+    const float* P = fu->cam.projection;
 
-    bool keep = !(cp[3] <= 0.0f);
-    float nx = 0.f, ny = 0.f, nz = 0.f;
-    if (keep) {
-      nx = cp[0] / cp[3];
-      ny = cp[1] / cp[3];
-      nz = cp[2] / cp[3];
-      keep = !(nx < -1.0f || nx > 1.0f || ny < -1.0f || ny > 1.0f || nz < 0.0f || nz > 1.0f);
-    }
-    if (keep) {
-      const float W = __ldg(&fu->cam.viewport[0]);
-      const float H = __ldg(&fu->cam.viewport[1]);
-      const float sx = (nx * 0.5f + 0.5f) * W;
-      const float sy = (1.0f - (ny * 0.5f + 0.5f)) * H;
+    bool valid = false;
+    float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
+    uint4 r3 = make_uint4(0u, 0u, 0u, 0u);
+    uint32_t count = 0;
 
-      const float qw = q.x, qx = q.y, qy = q.z, qz = q.w;
-      const float xx = qx * qx, yy = qy * qy, zz = qz * qz;
-      const float xy = qx * qy, xz = qx * qz, yz = qy * qz;
-      const float wx = qw * qx, wy = qw * qy, wz = qw * qz;
-      float R[3][3];  // [col][row]
-      R[0][0] = 1.0f - 2.0f * (yy + zz); R[0][1] = 2.0f * (xy + wz);        R[0][2] = 2.0f * (xz - wy);
-      R[1][0] = 2.0f * (xy - wz);        R[1][1] = 1.0f - 2.0f * (xx + zz); R[1][2] = 2.0f * (yz + wx);
-      R[2][0] = 2.0f * (xz + wy);        R[2][1] = 2.0f * (yz - wx);        R[2][2] = 1.0f - 2.0f * (xx + yy);
-      const float sc[3] = {s.x, s.y, s.z};
-      float M[3][3];
+    if (active) {
+      float vp[4], cp[4];
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
+      for (int r = 0; r < 4; ++r)
+        vp[r] = __ldg(V + 0 * 4 + r) * p.x + __ldg(V + 1 * 4 + r) * p.y +
+                __ldg(V + 2 * 4 + r) * p.z + __ldg(V + 3 * 4 + r) * 1.0f;
 #pragma unroll
-        for (int r = 0; r < 3; ++r) M[k][r] = R[k][r] * sc[k];
-      float S[3][3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-          S[a][b] = M[0][a] * M[0][b] + M[1][a] * M[1][b] + M[2][a] * M[2][b];
+      for (int r = 0; r < 4; ++r)
+        cp[r] = __ldg(P + 0 * 4 + r) * vp[0] + __ldg(P + 1 * 4 + r) * vp[1] +
+                __ldg(P + 2 * 4 + r) * vp[2] + __ldg(P + 3 * 4 + r) * vp[3];
 
-      const float fx = __ldg(P + 0) * W * 0.5f;
-      const float fy = __ldg(P + 5) * H * 0.5f;
-      const float z_cam = -vp[2];
-      const float inv_z = 1.0f / z_cam;
-      const float inv_z2 = inv_z * inv_z;
-      float J[2][3];
-      J[0][0] = fx * inv_z;  J[0][1] = 0.0f;        J[0][2] = fx * vp[0] * inv_z2;
-      J[1][0] = 0.0f;        J[1][1] = -fy * inv_z; J[1][2] = -fy * vp[1] * inv_z2;
-      float T[2][3];
-#pragma unroll
-      for (int r = 0; r < 2; ++r)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-          T[r][j] = J[r][0] * __ldg(V + j * 4 + 0) + J[r][1] * __ldg(V + j * 4 + 1) +
-                    J[r][2] * __ldg(V + j * 4 + 2);
-      float A[2][3];
-#pragma unroll
-      for (int r = 0; r < 2; ++r)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-          A[r][j] = T[r][0] * S[0][j] + T[r][1] * S[1][j] + T[r][2] * S[2][j];
-      const float c00 = A[0][0] * T[0][0] + A[0][1] * T[0][1] + A[0][2] * T[0][2];
-      const float c10 = A[1][0] * T[0][0] + A[1][1] * T[0][1] + A[1][2] * T[0][2];
-      const float c11 = A[1][0] * T[1][0] + A[1][1] * T[1][1] + A[1][2] * T[1][2];
+      bool keep = !(cp[3] <= 0.0f);
+      float nx = 0.f, ny = 0.f, nz = 0.f;
+      if (keep) {
+        nx = cp[0] / cp[3];
+        ny = cp[1] / cp[3];
+        nz = cp[2] / cp[3];
+        keep = !(nx < -1.0f || nx > 1.0f || ny < -1.0f || ny > 1.0f || nz < 0.0f || nz > 1.0f);
+      }
+      if (keep) {
+        const float W = __ldg(&fu->cam.viewport[0]);
+        const float H = __ldg(&fu->cam.viewport[1]);
+        const float sx = (nx * 0.5f + 0.5f) * W;
+        const float sy = (1.0f - (ny * 0.5f + 0.5f)) * H;
 
-      const float a = c00 + 0.3f;
-      const float b = c10;
-      const float c = c11 + 0.3f;
-      const float det = a * c - b * b;
-      if (!(det <= 0.0f)) {
-        const float inv_det = 1.0f / det;
-        const float mid = 0.5f * (a + c);
-        const float lambda = mid + sqrtf(fmaxf(0.1f, mid * mid - det));
-        const float radius = fmaxf(2.0f, ceilf(3.0f * sqrtf(lambda)));
-        const float minx = fmaxf(0.0f, sx - radius);
-        const float miny = fmaxf(0.0f, sy - radius);
-        const float maxx = fminf(W - 1.0f, sx + radius);
-        const float maxy = fminf(H - 1.0f, sy + radius);
-        const float itx = __ldg(&fu->inv_tile[0]), ity = __ldg(&fu->inv_tile[1]);
-        const uint32_t lastx = __ldg(&fu->tile_count[0]) - 1u;
-        const uint32_t lasty = __ldg(&fu->tile_count[1]) - 1u;
-        const uint32_t tminx = min(__float2uint_rz(floorf(minx * itx)), lastx);
-        const uint32_t tminy = min(__float2uint_rz(floorf(miny * ity)), lasty);
-        const uint32_t tmaxx = min(__float2uint_rz(floorf(maxx * itx)), lastx);
-        const uint32_t tmaxy = min(__float2uint_rz(floorf(maxy * ity)), lasty);
-        if (!(tminx > tmaxx || tminy > tmaxy)) {
-          valid = true;
-          count = (tmaxx - tminx + 1u) * (tmaxy - tminy + 1u);
-          r0 = make_float4(sx, sy, vp[2], radius);
-          r1 = make_float4(c * inv_det, -b * inv_det, a * inv_det, col.w);
-          r2 = make_float4(col.x, col.y, col.z, 0.0f);
-          r3 = make_uint4(tminx, tminy, tmaxx, tmaxy);
+        const float fx = __ldg(P + 0) * W * 0.5f;
+        const float fy = __ldg(P + 5) * H * 0.5f;
+        const float z_cam = -vp[2];
+        const float inv_z = 1.0f / z_cam;
+        const float inv_z2 = inv_z * inv_z;
+        float J[2][3];
+        J[0][0] = fx * inv_z;  J[0][1] = 0.0f;        J[0][2] = fx * vp[0] * inv_z2;
+        J[1][0] = 0.0f;        J[1][1] = -fy * inv_z; J[1][2] = -fy * vp[1] * inv_z2;
+        float T[2][3];
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            T[r][j] = J[r][0] * __ldg(V + j * 4 + 0) + J[r][1] * __ldg(V + j * 4 + 1) +
+                      J[r][2] * __ldg(V + j * 4 + 2);
+        float A[2][3];
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            A[r][j] = T[r][0] * S[0][j] + T[r][1] * S[1][j] + T[r][2] * S[2][j];
+        const float c00 = A[0][0] * T[0][0] + A[0][1] * T[0][1] + A[0][2] * T[0][2];
+        const float c10 = A[1][0] * T[0][0] + A[1][1] * T[0][1] + A[1][2] * T[0][2];
+        const float c11 = A[1][0] * T[1][0] + A[1][1] * T[1][1] + A[1][2] * T[1][2];
+
+        const float a = c00 + 0.3f;
+        const float b = c10;
+        const float c = c11 + 0.3f;
+        const float det = a * c - b * b;
+        if (!(det <= 0.0f)) {
+          const float inv_det = 1.0f / det;
+          const float mid = 0.5f * (a + c);
+          const float lambda = mid + sqrtf(fmaxf(0.1f, mid * mid - det));
+          const float radius = fmaxf(2.0f, ceilf(3.0f * sqrtf(lambda)));
+          const float minx = fmaxf(0.0f, sx - radius);
+          const float miny = fmaxf(0.0f, sy - radius);
+          const float maxx = fminf(W - 1.0f, sx + radius);
+          const float maxy = fminf(H - 1.0f, sy + radius);
+          const float itx = __ldg(&fu->inv_tile[0]), ity = __ldg(&fu->inv_tile[1]);
+          const uint32_t lastx = __ldg(&fu->tile_count[0]) - 1u;
+          const uint32_t lasty = __ldg(&fu->tile_count[1]) - 1u;
+          const uint32_t tminx = min(__float2uint_rz(floorf(minx * itx)), lastx);
+          const uint32_t tminy = min(__float2uint_rz(floorf(miny * ity)), lasty);
+          const uint32_t tmaxx = min(__float2uint_rz(floorf(maxx * itx)), lastx);
+          const uint32_t tmaxy = min(__float2uint_rz(floorf(maxy * ity)), lasty);
+          if (!(tminx > tmaxx || tminy > tmaxy)) {
+            valid = true;
+            count = (tmaxx - tminx + 1u) * (tmaxy - tminy + 1u);
+            r0 = make_float4(sx, sy, vp[2], radius);
+            r1 = make_float4(c * inv_det, -b * inv_det, a * inv_det, col.w);
+            r2 = make_float4(col.x, col.y, col.z, 0.0f);
+            r3 = make_uint4(tminx, tminy, tmaxx, tmaxy);
+          }
         }
       }
     }
-  }
 
-  if (DEG > 0) {
-    if (bulk && !mbar_wait(s_bar, 0)) {
-      if (threadIdx.x == 0) latch_error(err, DEVERR_TIMEOUT);
-      valid = false;
+    if (DEG > 0) {
+      if (!sh_ready) valid = false;
+      if (valid) {
+        float cc[3];
+        sh_color<DEG>(p.x, p.y, p.z, fu->cam.position, col, s_sh + threadIdx.x * KC, cc);
+        r2.x = cc[0];
+        r2.y = cc[1];
+        r2.z = cc[2];
+      }
     }
-    if (valid) {
-      float cc[3];
-      sh_color<DEG>(p.x, p.y, p.z, fu->cam.position, col, s_sh + threadIdx.x * KC, cc);
-      r2.x = cc[0];
-      r2.y = cc[1];
-      r2.z = cc[2];
-    }
-  }
 
-  if (active) {
-    if (!valid) {
-      r0 = r1 = r2 = make_float4(0.f, 0.f, 0.f, 0.f);
-      r3 = make_uint4(0u, 0u, 0u, 0u);
-      count = 0u;
-    } else {
-      r2.w = __uint_as_float(1u);
-    }
-    float4* o = reinterpret_cast<float4*>(out + gi);
-    o[0] = r0;
-    o[1] = r1;
-    o[2] = r2;
-    reinterpret_cast<uint4*>(o)[3] = r3;
-    counts[gi] = count;
-    if (depth_keys != nullptr) {  // per-splat depth sort keys of the fused rebin
-      depth_keys[gi] = valid ? __float_as_uint(-r0.z) : 0xffffffffu;
-      depth_ids[gi] = gi;
+    if (active) {
+      if (!valid) {
+        r0 = r1 = r2 = make_float4(0.f, 0.f, 0.f, 0.f);
+        r3 = make_uint4(0u, 0u, 0u, 0u);
+        count = 0u;
+      } else {
+        r2.w = __uint_as_float(1u);
+      }
+      float4* o = reinterpret_cast<float4*>(out + gi);
+      o[0] = r0;
+      o[1] = r1;
+      o[2] = r2;
+      reinterpret_cast<uint4*>(o)[3] = r3;
+      counts[gi] = count;
+      if (depth_keys != nullptr) {  // per-splat depth sort keys of the fused rebin
+        depth_keys[gi] = valid ? __float_as_uint(-r0.z) : 0xffffffffu;
+        depth_ids[gi] = gi;
+      }
     }
   }
 }
@@ -272,6 +287,8 @@ __global__ void __launch_bounds__(kThreads)
                       uint32_t* __restrict__ err) {
   extern __shared__ __align__(16) float s_sh[];
   __shared__ uint64_t s_bar;
+  // block_base counts the blocks of the scene groups' leaders only, so the
+  // search lands on the leader of this block's group
   const uint32_t v =
       find_view(n_views, blockIdx.x, [&](uint32_t i) { return __ldg(&views[i].block_base); });
   const ViewDesc& vd = views[v];
@@ -279,21 +296,22 @@ __global__ void __launch_bounds__(kThreads)
   const uint32_t deg = vd.sh == nullptr ? 0u : min(vd.sh_degree, (uint32_t)MAXDEG);
   switch (deg) {  // uniform per block
     case 0:
-      preprocess_block<0>(vd, local_first, s_sh, &s_bar, out, counts, depth_keys, depth_ids, err);
+      preprocess_block<0>(views, v, local_first, s_sh, &s_bar, out, counts, depth_keys,
+                          depth_ids, err);
       break;
     case 1:
       if (MAXDEG >= 1)
-        preprocess_block<MAXDEG >= 1 ? 1 : 0>(vd, local_first, s_sh, &s_bar, out, counts,
+        preprocess_block<MAXDEG >= 1 ? 1 : 0>(views, v, local_first, s_sh, &s_bar, out, counts,
                                               depth_keys, depth_ids, err);
       break;
     case 2:
       if (MAXDEG >= 2)
-        preprocess_block<MAXDEG >= 2 ? 2 : 0>(vd, local_first, s_sh, &s_bar, out, counts,
+        preprocess_block<MAXDEG >= 2 ? 2 : 0>(views, v, local_first, s_sh, &s_bar, out, counts,
                                               depth_keys, depth_ids, err);
       break;
     default:
       if (MAXDEG >= 3)
-        preprocess_block<MAXDEG >= 3 ? 3 : 0>(vd, local_first, s_sh, &s_bar, out, counts,
+        preprocess_block<MAXDEG >= 3 ? 3 : 0>(views, v, local_first, s_sh, &s_bar, out, counts,
                                               depth_keys, depth_ids, err);
       break;
   }
