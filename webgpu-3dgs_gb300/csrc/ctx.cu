@@ -576,7 +576,8 @@ int fused_rebin(gs3d_ctx* c) {
   {
     StageScope t(c, GS3D_STAGE_EMIT);
     CK(launch_emit_sorted(dviews(c), nv, c->total_splats,
-                          static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->depth_ids_a),
+                          static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->depth_keys_a),
+                          u32(c->depth_ids_a),
                           u32(c->sorted_offsets), u32(c->ref_counter), c->capacity,
                           static_cast<uint2*>(c->keys_a.p), u32(c->vals_a), tp,
                           &k->tile_hist[0][0], &k->error, c->stream),

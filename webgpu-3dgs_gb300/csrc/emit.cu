@@ -91,6 +91,7 @@ template <int TP, int BINS>
 __global__ void __launch_bounds__(kThreads)
     emit_sorted_kernel(const ViewDesc* __restrict__ views, uint32_t n_views, uint32_t n,
                        const gs3d_projected_splat* __restrict__ proj,
+                       const uint32_t* __restrict__ sorted_keys,
                        const uint32_t* __restrict__ sorted_ids,
                        const uint32_t* __restrict__ sorted_offsets,
                        const uint32_t* __restrict__ ref_counter, uint32_t capacity,
@@ -111,9 +112,10 @@ __global__ void __launch_bounds__(kThreads)
   const uint32_t first = blockIdx.x * kThreads;
   const uint32_t i = first + threadIdx.x;
   if (i < n) {
+    // only the tile rectangle is gathered (one 32-byte sector of the record):
+    // the depth bits come in order from the depth sort, the ref count from
+    // the scan's offsets (0 for culled splats, whose rectangle is zeroed)
     const uint32_t id = __ldg(sorted_ids + i);
-    const float4 r0 = __ldg(reinterpret_cast<const float4*>(proj + id));
-    const uint32_t valid = __ldg(&proj[id].valid);
     const uint4 r3 = __ldg(reinterpret_cast<const uint4*>(proj + id) + 3);
     const uint32_t w = r3.z - r3.x + 1u, h = r3.w - r3.y + 1u;
     const uint32_t v =
@@ -122,8 +124,8 @@ __global__ void __launch_bounds__(kThreads)
     s_tminx[threadIdx.x] = r3.x;
     s_tminy[threadIdx.x] = r3.y;
     s_w[threadIdx.x] = w;
-    s_cnt[threadIdx.x] = valid ? w * h : 0u;
-    s_lo[threadIdx.x] = __float_as_uint(-r0.z);
+    s_cnt[threadIdx.x] = w * h;
+    s_lo[threadIdx.x] = __ldg(sorted_keys + i);
     s_id[threadIdx.x] = id;
     s_tx[threadIdx.x] = __ldg(&views[v].f.tile_count[0]);
     s_tb[threadIdx.x] = __ldg(&views[v].f.tile_base);
@@ -177,7 +179,8 @@ __global__ void __launch_bounds__(kThreads)
 }  // namespace
 
 cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t n,
-                               const gs3d_projected_splat* proj, const uint32_t* sorted_ids,
+                               const gs3d_projected_splat* proj, const uint32_t* sorted_keys,
+                               const uint32_t* sorted_ids,
                                const uint32_t* sorted_offsets, const uint32_t* ref_counter,
                                uint32_t capacity, uint2* keys, uint32_t* values,
                                const SortPlan& tile_plan, uint32_t* g_hist, uint32_t* err,
@@ -197,7 +200,8 @@ cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t
 #define GS3D_EMIT_CASE(TP, BINS)                                                              \
   case TP:                                                                                    \
     emit_sorted_kernel<TP, BINS><<<blocks, kThreads, 0, s>>>(                                 \
-        views, n_views, n, proj, sorted_ids, sorted_offsets, ref_counter, capacity, keys,     \
+        views, n_views, n, proj, sorted_keys, sorted_ids, sorted_offsets, ref_counter,        \
+        capacity, keys,                                                                       \
         values, sh, mk, g_hist, err);                                                         \
     break;
   if (wide) {

@@ -300,7 +300,8 @@ cudaError_t launch_log_costs(const uint32_t* costs, uint32_t n, float* out, cuda
 // Emit in depth-sorted order over all splat-views of a batch (global tile
 // ids, global splat-view values) + histograms of the tile-id digit places.
 cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t total,
-                               const gs3d_projected_splat* proj, const uint32_t* sorted_ids,
+                               const gs3d_projected_splat* proj, const uint32_t* sorted_keys,
+                               const uint32_t* sorted_ids,
                                const uint32_t* sorted_offsets, const uint32_t* ref_counter,
                                uint32_t capacity, uint2* keys, uint32_t* values,
                                const SortPlan& tile_plan, uint32_t* g_hist, uint32_t* err,
