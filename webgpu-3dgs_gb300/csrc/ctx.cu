@@ -59,6 +59,10 @@ struct gs3d_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // splat-target copy-outs run on their own stream; the next raster (the only
+  // writer of the target) waits for the last one (copy_done)
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t frame_done = nullptr, copy_done = nullptr;
   int sm_count = 0;
   std::string err = "no error";
 
@@ -167,6 +171,7 @@ int ensure(gs3d_ctx* c, DevBuf& b, size_t bytes, const char* name) {
   if (b.bytes >= bytes) return GS3D_OK;
   if (b.p) {
     CK(cudaStreamSynchronize(c->stream), "synchronize before resize");
+    if (c->copy_stream) CK(cudaStreamSynchronize(c->copy_stream), "copy-outs before resize");
     release(b);
   }
   void* p = nullptr;
@@ -293,6 +298,7 @@ struct StageScope {
 
 int sync_and_check(gs3d_ctx* c) {
   CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  if (c->copy_stream) CK(cudaStreamSynchronize(c->copy_stream), "copy-out stream");
   return check_device_errors(c);
 }
 
@@ -533,6 +539,13 @@ int raster_stage(gs3d_ctx* c, bool culled) {
   a.batch = c->raster_batch;
   a.culled = culled;
   CK(cudaMemsetAsync(a.queue_counter, 0, sizeof(uint32_t), c->stream), "reset raster queue");
+  // the previous frame's splat target may still be copying out (captured as
+  // an external event wait in graph mode; a never-recorded event is no wait)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(c->stream, &cap), "capture status");
+  CK(cudaStreamWaitEvent(c->stream, c->copy_done,
+                         cap == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0),
+     "wait for the previous copy-out");
   CK(launch_raster(a, c->sm_count, c->stream), "rasterize_tiles");
   return GS3D_OK;
 }
@@ -733,6 +746,10 @@ int gs3d_create(gs3d_ctx** out, const gs3d_config* cfg) {
   }
   probe_kernel<<<1, 1, 0, c->stream>>>(nullptr);
   if (cudaGetLastError() != cudaSuccess) return bail(GS3D_ERR_NO_DEVICE);
+  if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->frame_done, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming) != cudaSuccess)
+    return bail(GS3D_ERR_CUDA);
   c->scenes.resize(1);
   if (ensure(c, c->ctrl, sizeof(Ctrl), "control block") != GS3D_OK ||
       ensure(c, c->ref_counter, 16, "ref_counter") != GS3D_OK)
@@ -777,6 +794,12 @@ int gs3d_destroy(gs3d_ctx* c) {
   if (c->graph.h_views) cudaFreeHost(c->graph.h_views);
   if (c->h_upload) cudaFreeHost(c->h_upload);
   if (c->h_word) cudaFreeHost(c->h_word);
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
+  if (c->frame_done) cudaEventDestroy(c->frame_done);
+  if (c->copy_done) cudaEventDestroy(c->copy_done);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return GS3D_OK;
@@ -1412,6 +1435,7 @@ int gs3d_write_buffer(gs3d_ctx* c, gs3d_buffer which, const void* src, size_t by
   if (bytes && !src) return fail(c, GS3D_ERR_INVALID_ARG, "null source");
   TRY(set_device(c));
   CK(cudaStreamSynchronize(c->stream), "synchronize before copy-in");
+  CK(cudaStreamSynchronize(c->copy_stream), "copy-outs before copy-in");
   if (bytes) CK(cudaMemcpy(b->p, src, bytes, cudaMemcpyHostToDevice), "copy-in");
   return GS3D_OK;
 }
@@ -1425,8 +1449,17 @@ int gs3d_copy_buffer_async(gs3d_ctx* c, gs3d_buffer which, void* dst, size_t byt
                 b->bytes);
   if (bytes && !dst) return fail(c, GS3D_ERR_INVALID_ARG, "null destination");
   TRY(set_device(c));
-  if (bytes)
-    CK(cudaMemcpyAsync(dst, b->p, bytes, cudaMemcpyDeviceToHost, c->stream), "async copy-out");
+  if (!bytes) return GS3D_OK;
+  if (which == GS3D_BUF_SPLAT_TARGET) {
+    // off the rebin stream: the next rebin runs while this frame copies out
+    CK(cudaEventRecord(c->frame_done, c->stream), "frame event");
+    CK(cudaStreamWaitEvent(c->copy_stream, c->frame_done, 0), "copy waits for the frame");
+    CK(cudaMemcpyAsync(dst, b->p, bytes, cudaMemcpyDeviceToHost, c->copy_stream),
+       "async copy-out");
+    CK(cudaEventRecord(c->copy_done, c->copy_stream), "copy event");
+    return GS3D_OK;
+  }
+  CK(cudaMemcpyAsync(dst, b->p, bytes, cudaMemcpyDeviceToHost, c->stream), "async copy-out");
   return GS3D_OK;
 }
 
