@@ -122,6 +122,44 @@ __device__ __forceinline__ bool blend_one(float pfx, float pfy, const SplatStage
   return blend_alpha(p, s.c, alpha, ok && live);
 }
 
+// Two pixels of one column in the halves of a float2 (the two-pixel
+// variant).  Every component is computed by the scalar operation of
+// splat_alpha / blend_alpha, in the same order and rounding (the paired
+// FP32 instructions of sm_100 round each half like their scalar forms), so
+// each pixel is bit-identical to the one-pixel variants.
+__device__ __forceinline__ float2 bcast(float x) { return make_float2(x, x); }
+
+struct Pixel2 {
+  float2 cr, cg, cb, T;
+};
+
+__device__ __forceinline__ float2 splat_alpha2(float pfx, float2 pfy, const SplatStage& s,
+                                               bool& ok0, bool& ok1) {
+  const float4 a = s.a, b = s.b;
+  const float dx = pfx - a.x;
+  const float2 dy = __fadd2_rn(pfy, bcast(-a.y));
+  const float2 d2 = __ffma2_rn(bcast(dx), bcast(dx), __fmul2_rn(dy, dy));
+  const float2 q = __ffma2_rn(bcast(b.x * dx), bcast(dx),
+                              __ffma2_rn(bcast(b.y * dx), dy,
+                                         __fmul2_rn(__fmul2_rn(bcast(b.z), dy), dy)));
+  const float2 e = make_float2(ex2_approx(-q.x), ex2_approx(-q.y));
+  const float2 am = __fmul2_rn(bcast(a.w), e);
+  const float2 alpha = make_float2(fminf(0.99f, am.x), fminf(0.99f, am.y));
+  ok0 = (d2.x <= a.z) && (q.x >= 0.0f) && (alpha.x >= 1.0f / 255.0f);
+  ok1 = (d2.y <= a.z) && (q.y >= 0.0f) && (alpha.y >= 1.0f / 255.0f);
+  return alpha;
+}
+
+__device__ __forceinline__ void blend_alpha2(Pixel2& p, const float4 c, float2 alpha, bool ok0,
+                                             bool ok1) {
+  const float2 al = make_float2(ok0 ? alpha.x : 0.0f, ok1 ? alpha.y : 0.0f);
+  const float2 ta = __fmul2_rn(p.T, al);
+  p.cr = __ffma2_rn(ta, bcast(c.x), p.cr);
+  p.cg = __ffma2_rn(ta, bcast(c.y), p.cg);
+  p.cb = __ffma2_rn(ta, bcast(c.z), p.cb);
+  p.T = __fmul2_rn(p.T, __fadd2_rn(bcast(1.0f), make_float2(-al.x, -al.y)));
+}
+
 __device__ __forceinline__ void store_pixel(uint2* image, uint32_t W, uint32_t px, uint32_t py,
                                             const Pixel& p) {
   const __half2 rg = __floats2half2_rn(p.cr, p.cg);
@@ -375,7 +413,8 @@ __device__ void raster_tile_culled2(const RasterArgs& a, const TileGeom& g, Spla
   const uint32_t len = end > start ? end - start : 0u;
   const uint32_t nbatches = (len + D - 1) / D;
 
-  Pixel p0{0.f, 0.f, 0.f, 1.0f}, p1{0.f, 0.f, 0.f, 1.0f};
+  const float2 pfy = make_float2(pfy0, pfy1);
+  Pixel2 p{bcast(0.f), bcast(0.f), bcast(0.f), bcast(1.0f)};
   bool done0 = !in0, done1 = !in1;
   uint32_t used0 = 0, used1 = 0;
 
@@ -401,13 +440,15 @@ __device__ void raster_tile_culled2(const RasterArgs& a, const TileGeom& g, Spla
           mask &= mask - 1;
           const SplatStage& sp = cur[k0 + b];
           bool ok0, ok1;
-          const float al0 = splat_alpha(pfx, pfy0, sp, ok0);
-          const float al1 = splat_alpha(pfx, pfy1, sp, ok1);
-          if (blend_alpha(p0, sp.c, al0, ok0 && !done0)) {
+          const float2 al = splat_alpha2(pfx, pfy, sp, ok0, ok1);
+          ok0 = ok0 && !done0;
+          ok1 = ok1 && !done1;
+          blend_alpha2(p, sp.c, al, ok0, ok1);
+          if (ok0 && p.T.x < 1.0e-4f) {
             done0 = true;
             used0 = bi * D + k0 + b + 1;
           }
-          if (blend_alpha(p1, sp.c, al1, ok1 && !done1)) {
+          if (ok1 && p.T.y < 1.0e-4f) {
             done1 = true;
             used1 = bi * D + k0 + b + 1;
           }
@@ -424,11 +465,11 @@ __device__ void raster_tile_culled2(const RasterArgs& a, const TileGeom& g, Spla
   }
   if (in0) {
     atomicMax(s_cost, used0);
-    store_pixel(g.image, g.W, px, py0, p0);
+    store_pixel(g.image, g.W, px, py0, Pixel{p.cr.x, p.cg.x, p.cb.x, p.T.x});
   }
   if (in1) {
     atomicMax(s_cost, used1);
-    store_pixel(g.image, g.W, px, py1, p1);
+    store_pixel(g.image, g.W, px, py1, Pixel{p.cr.y, p.cg.y, p.cb.y, p.T.y});
   }
 }
 
