@@ -326,6 +326,7 @@ struct RasterArgs {
   uint32_t* queue_counter;
   uint32_t batch;         // splats staged per batch (0 = tile_w * tile_h)
   bool culled;
+  uint32_t split;         // CTAs per tile (row strips), set by launch_raster
 };
 cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s);
 

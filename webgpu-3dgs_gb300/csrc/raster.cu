@@ -388,15 +388,16 @@ __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, Splat
 // and looped over once for 64 pixels.  blockDim.x == tile_w * tile_h / 2;
 // tile sides divide by 8.  Per pixel the arithmetic and the splat sequence
 // are those of the other variants (bit-identical image).
-__device__ void raster_tile_culled2(const RasterArgs& a, const TileGeom& g, SplatStage* buf0,
-                                    SplatStage* buf1, uint32_t* s_cost) {
+__device__ void raster_tile_culled2(const RasterArgs& a, const TileGeom& g, uint32_t strip,
+                                    SplatStage* buf0, SplatStage* buf1, uint32_t* s_cost) {
   const uint32_t nt = a.tile_w * a.tile_h;
-  const uint32_t nthr = nt / 2;
+  const uint32_t strip_h = a.tile_h / a.split;  // this CTA shades rows [strip * strip_h, +strip_h)
+  const uint32_t nthr = a.tile_w * strip_h / 2;
   const uint32_t D = a.batch ? a.batch : nt;  // splats per staged batch
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t bw = a.tile_w / 8;
   const uint32_t px = g.ox + (warp % bw) * 8 + (lane & 7);
-  const uint32_t py0 = g.oy + (warp / bw) * 8 + (lane >> 3), py1 = py0 + 4;
+  const uint32_t py0 = g.oy + strip * strip_h + (warp / bw) * 8 + (lane >> 3), py1 = py0 + 4;
   const bool in0 = px < g.W && py0 < g.H, in1 = px < g.W && py1 < g.H;
   const float pfx = (float)px + 0.5f, pfy0 = (float)py0 + 0.5f, pfy1 = (float)py1 + 0.5f;
   float xlo = pfx, xhi = pfx, ylo = pfy0, yhi = pfy1;
@@ -490,17 +491,23 @@ __device__ __forceinline__ void raster_loop(const RasterArgs& a) {
     }
     __syncthreads();
     const uint32_t item = s_item;
-    if (item >= a.num_tiles) break;
-    const uint32_t t = a.order != nullptr ? __ldg(a.order + item) : item;
+    if (item >= a.num_tiles * a.split) break;
+    const uint32_t ti = item / a.split, strip = item - ti * a.split;
+    const uint32_t t = a.order != nullptr ? __ldg(a.order + ti) : ti;
     const TileGeom g = tile_geom(a, t);
     if (MODE == 2)
-      raster_tile_culled2(a, g, buf0, buf1, &s_cost);
+      raster_tile_culled2(a, g, strip, buf0, buf1, &s_cost);
     else if (MODE == 1)
       raster_tile_culled(a, g, buf0, buf1, &s_cost);
     else
       raster_tile_plain(a, g, buf0, buf1, &s_cost);
     __syncthreads();  // s_cost complete; shared buffers free for the next tile
-    if (threadIdx.x == 0 && a.tile_costs != nullptr) a.tile_costs[t] = s_cost;
+    if (threadIdx.x == 0 && a.tile_costs != nullptr) {
+      if (a.split == 1)
+        a.tile_costs[t] = s_cost;
+      else
+        atomicMax(a.tile_costs + t, s_cost);  // zeroed before the launch
+    }
   }
 }
 
@@ -513,22 +520,31 @@ __global__ void __launch_bounds__(512, 2) raster_kernel_culled2(RasterArgs a) {
 
 }  // namespace
 
-cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s) {
-  if (a.num_tiles == 0) return cudaSuccess;
+cudaError_t launch_raster(const RasterArgs& args, int sm_count, cudaStream_t s) {
+  if (args.num_tiles == 0) return cudaSuccess;
+  RasterArgs a = args;
   const uint32_t nt = a.tile_w * a.tile_h;
   if (a.batch % 32 != 0 || a.batch > 1024) return cudaErrorInvalidValue;
   const uint32_t D = a.batch ? a.batch : nt;
   const bool culled = a.culled && (nt % 32 == 0);
   // two pixels a thread where the tile splits into 8x8 blocks
   const int mode = !culled ? 0 : (a.tile_w % 8 == 0 && a.tile_h % 8 == 0) ? 2 : 1;
-  const uint32_t threads = mode == 2 ? nt / 2 : nt;
+  // two-pixel tiles of more than 512 pixels are shaded by two CTAs (row
+  // strips), so that a block barrier waits for at most eight warps
+  a.split = (mode == 2 && nt > 512 && (a.tile_h / 2) % 8 == 0) ? 2u : 1u;
+  const uint32_t threads = mode == 2 ? nt / (2 * a.split) : nt;
+  if (a.split > 1 && a.tile_costs != nullptr) {
+    const cudaError_t e =
+        cudaMemsetAsync(a.tile_costs, 0, (size_t)a.num_tiles * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+  }
   const size_t smem = 2 * (size_t)D * sizeof(SplatStage);
   auto kern = mode == 2 ? raster_kernel_culled2 : mode == 1 ? raster_kernel_culled
                                                              : raster_kernel_plain;
   // launch configuration per (variant, tile area, batch), computed once per process
   static std::mutex mu;
   static std::map<uint64_t, int> cache;
-  const uint64_t key = ((uint64_t)mode << 40) | ((uint64_t)nt << 20) | D;
+  const uint64_t key = ((uint64_t)mode << 40) | ((uint64_t)threads << 20) | D;
   int per_sm = 0;
   {
     std::lock_guard<std::mutex> lock(mu);
@@ -549,7 +565,7 @@ cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s) {
     cache[key] = per_sm;
   }
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
-      a.num_tiles, (uint64_t)sm_count * (uint64_t)std::max(per_sm, 1));
+      (uint64_t)a.num_tiles * a.split, (uint64_t)sm_count * (uint64_t)std::max(per_sm, 1));
   kern<<<grid, threads, smem, s>>>(a);
   return cudaGetLastError();
 }
