@@ -27,6 +27,10 @@
 //    alpha below 1/255, with margins that cover f32 rounding.  Pixels
 //    therefore blend exactly the same splats in the same order, and the
 //    image is bit-identical to the one-thread-per-pixel variant;
+//  * (two-pixel variant, tiles whose sides divide by 8) each warp owns an 8x8
+//    block, a lane shading rows y and y + 4 of one column with the paired
+//    FP32 instructions of sm_100 (each half rounded like the scalar path);
+//    tiles above 512 pixels are shaded by several CTAs, one row strip each;
 //  * each CTA records the tile's cost: the number of splats iterated before
 //    its last pixel terminated.
 //
@@ -513,7 +517,7 @@ __device__ __forceinline__ void raster_loop(const RasterArgs& a) {
 
 __global__ void raster_kernel_plain(RasterArgs a) { raster_loop<0>(a); }
 __global__ void raster_kernel_culled(RasterArgs a) { raster_loop<1>(a); }
-// at most 512 threads (a 32x32 tile), two such CTAs per SM
+// at most 512 threads (a 1024-pixel tile of unsplittable strips)
 __global__ void __launch_bounds__(512, 2) raster_kernel_culled2(RasterArgs a) {
   raster_loop<2>(a);
 }
@@ -529,9 +533,11 @@ cudaError_t launch_raster(const RasterArgs& args, int sm_count, cudaStream_t s) 
   const bool culled = a.culled && (nt % 32 == 0);
   // two pixels a thread where the tile splits into 8x8 blocks
   const int mode = !culled ? 0 : (a.tile_w % 8 == 0 && a.tile_h % 8 == 0) ? 2 : 1;
-  // two-pixel tiles of more than 512 pixels are shaded by two CTAs (row
-  // strips), so that a block barrier waits for at most eight warps
-  a.split = (mode == 2 && nt > 512 && (a.tile_h / 2) % 8 == 0) ? 2u : 1u;
+  // two-pixel tiles of more than 512 pixels are shaded by four (else two)
+  // CTAs of row strips whose heights divide by 8, so that a block barrier
+  // waits for few warps and more CTAs interleave on an SM
+  a.split = 1;
+  if (mode == 2 && nt > 512) a.split = (a.tile_h / 4) % 8 == 0 ? 4u : (a.tile_h / 2) % 8 == 0 ? 2u : 1u;
   const uint32_t threads = mode == 2 ? nt / (2 * a.split) : nt;
   if (a.split > 1 && a.tile_costs != nullptr) {
     const cudaError_t e =
