@@ -143,25 +143,58 @@ __global__ void __launch_bounds__(kThreads)
   }
   const int sh[4] = {shifts.x, shifts.y, shifts.z, shifts.w};
   const uint32_t mk[4] = {masks.x, masks.y, masks.z, masks.w};
-  for (uint32_t base = begin; base < end; base += kThreads) {  // warp-uniform trip count
-    const uint32_t j = base + threadIdx.x;
-    bool live = j < end;
-    uint32_t tile = 0;
-    if (live) {
-      uint32_t lo = 0, hi = nloc;
+  // Each warp expands a contiguous share of the block's refs, 32 at a time.
+  // The owner of a ref is the last splat starting at or before it.  The
+  // owners of a 32-ref chunk are the owner c0 of its first ref and the
+  // splats c0+1 .. c0+32 starting inside it; while those starts are
+  // distinct (every valid splat has a ref, and culled splats, which have
+  // none, sort after all valid ones) one OR-reduction of their start bits
+  // gives every lane its owner.  A chunk with equal starts (zero-count
+  // splats) searches per ref instead.
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t share = ((end - begin + kThreads - 1) / kThreads) * 32u;
+  const uint32_t wbeg = min(end, begin + warp * share), wend = min(end, wbeg + share);
+  uint32_t c0 = 0;  // owner of ref wbeg: the last splat starting at or before it
+  {
+    uint32_t lo = 0, hi = nloc;  // invariant: s_off[lo] <= wbeg < s_off[hi]
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (s_off[mid] <= wbeg) lo = mid; else hi = mid;
+    }
+    c0 = lo;
+  }
+  for (uint32_t cb = wbeg; cb < wend; cb += 32) {  // warp-uniform trip count
+    const uint32_t j = cb + lane;
+    const uint32_t cand = c0 + 1 + lane;
+    const uint32_t st = cand <= nloc ? s_off[cand] : 0xffffffffu;
+    const uint32_t rel = st - cb;
+    const uint32_t down = __shfl_down_sync(0xffffffffu, st, 1);
+    const uint32_t next_st = lane < 31 ? down : (cand < nloc ? s_off[cand + 1] : 0xffffffffu);
+    uint32_t o;
+    if (!__any_sync(0xffffffffu, rel < 32 && next_st == st)) {
+      const uint32_t starts = __reduce_or_sync(0xffffffffu, rel < 32 ? 1u << rel : 0u);
+      o = c0 + __popc(starts & (0xffffffffu >> (31 - lane)));
+    } else {
+      uint32_t lo = c0, hi = nloc;  // s_off[c0] <= cb <= j
       while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
         if (s_off[mid] <= j) lo = mid; else hi = mid;
       }
-      const uint32_t k = j - s_off[lo];
-      if (k < s_cnt[lo]) {
+      o = lo;
+    }
+    c0 = __shfl_sync(0xffffffffu, o, 31);  // owner of the chunk's last ref
+    bool live = j < wend;
+    uint32_t tile = 0;
+    if (live) {
+      const uint32_t k = j - s_off[o];
+      if (k < s_cnt[o]) {
         // row = floor(k / w) by a float reciprocal: exact while k + w < 2^22
         // (k < w * h <= tiles of one view)
-        const uint32_t w = s_w[lo];
-        const uint32_t row = (uint32_t)(((float)k + 0.5f) * s_winv[lo]);
-        tile = s_tb[lo] + (s_tminy[lo] + row) * s_tx[lo] + s_tminx[lo] + (k - row * w);
-        keys[j] = make_uint2(tile, s_lo[lo]);
-        values[j] = s_id[lo];
+        const uint32_t w = s_w[o];
+        const uint32_t row = (uint32_t)(((float)k + 0.5f) * s_winv[o]);
+        tile = s_tb[o] + (s_tminy[o] + row) * s_tx[o] + s_tminx[o] + (k - row * w);
+        keys[j] = make_uint2(tile, s_lo[o]);
+        values[j] = s_id[o];
       } else {
         live = false;
       }
