@@ -72,6 +72,37 @@ def test_tuned_keys_match_the_oracle(renderer, oracle, tile, digit, batch):
     renderer.setTuning(16, 8, 0)
 
 
+@pytest.mark.parametrize("w,h", [(2048, 300), (2400, 300), (300, 2100)])
+def test_tile_grids_wider_than_256_match_the_oracle(renderer, oracle, w, h):
+    """Grids of more than 256 tiles on an axis keep the emit's tile
+    rectangles in the projected records instead of one-word rectangles
+    (2048 px at 8 px tiles is the largest one-word grid); keys, values and
+    ranges stay bit-exact, alone and batched with a view whose grid fits
+    the one-word form."""
+    tile = 8
+    data = scenes.scene_small(60_000, seed=13)
+    u = scenes.small_camera(w, h).getUniformData(w, h)
+    o = oracle.rebin(u, w, h, tile, tile, data.positions, data.scales, data.rotations,
+                     data.colors, data.sphericalHarmonics, data.sphericalHarmonicsDegree)
+    renderer.setSplatData(data)
+    renderer.setTuning(tile, 8, 0)
+    renderer.rebin(data.splatCount, -(-w // tile), -(-h // tile), w, h, u)
+    R = renderer.refCount()
+    assert R == o["ref_counter"]
+    assert np.array_equal(renderer.readBuffer("sort_keys_a", R), o["sort_keys_a"])
+    assert np.array_equal(renderer.readBuffer("sort_values_a", R), o["sort_values_a"])
+    assert np.array_equal(renderer.readBuffer("tile_offsets"), o["tile_offsets"])
+    img = renderer.readImage()
+    small = scenes.small_camera(640, 360).getUniformData(640, 360)
+    renderer.rebinBatch([(0, small, 640, 360), (0, u, w, h)])
+    assert np.array_equal(renderer.readViewImage(1).view(np.uint16), img.view(np.uint16))
+    renderer.rebinBatch([(0, small, 640, 360)])
+    alone = renderer.readViewImage(0)
+    renderer.rebinBatch([(0, small, 640, 360), (0, u, w, h)])
+    assert np.array_equal(renderer.readViewImage(0).view(np.uint16), alone.view(np.uint16))
+    renderer.setTuning(16, 8, 0)
+
+
 def test_autotune_applies_the_fastest_candidate(renderer):
     data = scenes.scene_clusters(200_000, seed=2, sh_degree=0)
     renderer.setSplatData(data)

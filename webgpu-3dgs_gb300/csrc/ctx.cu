@@ -82,6 +82,7 @@ struct gs3d_ctx {
   DevBuf scan_status, sort_status;
   uint32_t scan_epoch = 0;
   DevBuf depth_keys_a, depth_ids_a, depth_keys_b, depth_ids_b, sorted_offsets, depth_status;
+  DevBuf rect8;  // one-word tile rectangles per splat-view (fused rebin, small grids)
   DevBuf tile_offsets, image, tile_costs, composite_out;
   DevBuf sched_keys_a, sched_keys_b, sched_order_a, sched_order_b, sched_status;
   // cost model (learned schedule)
@@ -221,6 +222,7 @@ int ensure_splat_buffers(gs3d_ctx* c, uint32_t m) {
   TRY(ensure(c, c->depth_ids_b, md * 4, "depth ids"));
   TRY(ensure(c, c->sorted_offsets, ((size_t)m + 1) * 4, "depth-ordered offsets"));
   TRY(ensure(c, c->depth_status, sort_status_words(m, 4) * 4, "depth sort status"));
+  TRY(ensure(c, c->rect8, (size_t)m * 4, "tile rectangles"));
   return GS3D_OK;
 }
 
@@ -559,11 +561,16 @@ int fused_rebin(gs3d_ctx* c) {
   Ctrl* k = ctrl_of(c);
   const uint32_t nv = (uint32_t)c->views.size();
   CK(cudaMemsetAsync(c->ctrl.p, 0, sizeof(Ctrl), c->stream), "reset control block");
+  // tile rectangles fit one word when every view has at most 256 tiles per axis
+  bool small_grids = true;
+  for (const ViewDesc& v : c->views)
+    small_grids = small_grids && v.f.tile_count[0] <= 256 && v.f.tile_count[1] <= 256;
+  uint32_t* rect8 = small_grids ? u32(c->rect8) : nullptr;
   {
     StageScope t(c, GS3D_STAGE_PREPROCESS);
     CK(launch_preprocess(dviews(c), nv, c->total_blocks, c->max_sh,
                          static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->counts),
-                         u32(c->depth_keys_a), u32(c->depth_ids_a), &k->error, c->stream),
+                         u32(c->depth_keys_a), u32(c->depth_ids_a), rect8, &k->error, c->stream),
        "preprocess");
   }
   {
@@ -589,7 +596,7 @@ int fused_rebin(gs3d_ctx* c) {
   {
     StageScope t(c, GS3D_STAGE_EMIT);
     CK(launch_emit_sorted(dviews(c), nv, c->total_splats,
-                          static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->depth_keys_a),
+                          static_cast<gs3d_projected_splat*>(c->proj.p), rect8, u32(c->depth_keys_a),
                           u32(c->depth_ids_a),
                           u32(c->sorted_offsets), u32(c->ref_counter), c->capacity,
                           static_cast<uint2*>(c->keys_a.p), u32(c->vals_a), tp,
@@ -781,6 +788,7 @@ int gs3d_destroy(gs3d_ctx* c) {
                     &c->keys_a,        &c->vals_a,        &c->keys_b,        &c->vals_b,
                     &c->scan_status,   &c->sort_status,   &c->depth_keys_a,  &c->depth_ids_a,
                     &c->depth_keys_b,  &c->depth_ids_b,   &c->sorted_offsets, &c->depth_status,
+                    &c->rect8,
                     &c->tile_offsets,  &c->image,         &c->tile_costs,    &c->sched_keys_a,
                     &c->sched_keys_b,  &c->sched_order_a, &c->sched_order_b, &c->sched_status,
                     &c->d_views,       &c->ctrl,          &c->model_params,  &c->model_mean,
@@ -1018,7 +1026,7 @@ int gs3d_preprocess(gs3d_ctx* c) {
   StageScope t(c, GS3D_STAGE_PREPROCESS);
   CK(launch_preprocess(dviews(c), 1, c->total_blocks, c->max_sh,
                        static_cast<gs3d_projected_splat*>(c->proj.p), u32(c->counts), nullptr,
-                       nullptr, &ctrl_of(c)->error, c->stream),
+                       nullptr, nullptr, &ctrl_of(c)->error, c->stream),
      "preprocess");
   return GS3D_OK;
 }

@@ -91,6 +91,7 @@ template <int TP, int BINS>
 __global__ void __launch_bounds__(kThreads)
     emit_sorted_kernel(const ViewDesc* __restrict__ views, uint32_t n_views, uint32_t n,
                        const gs3d_projected_splat* __restrict__ proj,
+                       const uint32_t* __restrict__ rect8,
                        const uint32_t* __restrict__ sorted_keys,
                        const uint32_t* __restrict__ sorted_ids,
                        const uint32_t* __restrict__ sorted_offsets,
@@ -115,14 +116,28 @@ __global__ void __launch_bounds__(kThreads)
     // only the tile rectangle is gathered (one 32-byte sector of the record):
     // the depth bits come in order from the depth sort, the ref count from
     // the scan's offsets (0 for culled splats, whose rectangle is zeroed)
+    // (or, where every view's tile grid fits 8 bits, the 4-byte word of the
+    // preprocess's compact rectangle array, which stays in L2)
     const uint32_t id = __ldg(sorted_ids + i);
-    const uint4 r3 = __ldg(reinterpret_cast<const uint4*>(proj + id) + 3);
-    const uint32_t w = r3.z - r3.x + 1u, h = r3.w - r3.y + 1u;
+    uint32_t x0, y0, w, h;
+    if (rect8 != nullptr) {
+      const uint32_t rr = __ldg(rect8 + id);
+      x0 = rr & 0xffu;
+      y0 = (rr >> 8) & 0xffu;
+      w = ((rr >> 16) & 0xffu) + 1u;
+      h = (rr >> 24) + 1u;
+    } else {
+      const uint4 r3 = __ldg(reinterpret_cast<const uint4*>(proj + id) + 3);
+      x0 = r3.x;
+      y0 = r3.y;
+      w = r3.z - r3.x + 1u;
+      h = r3.w - r3.y + 1u;
+    }
     const uint32_t v =
         find_view(n_views, id, [&](uint32_t k) { return __ldg(&views[k].splat_base); });
     s_off[threadIdx.x] = __ldg(sorted_offsets + i);
-    s_tminx[threadIdx.x] = r3.x;
-    s_tminy[threadIdx.x] = r3.y;
+    s_tminx[threadIdx.x] = x0;
+    s_tminy[threadIdx.x] = y0;
     s_w[threadIdx.x] = w;
     s_cnt[threadIdx.x] = w * h;
     s_lo[threadIdx.x] = __ldg(sorted_keys + i);
@@ -212,7 +227,8 @@ __global__ void __launch_bounds__(kThreads)
 }  // namespace
 
 cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t n,
-                               const gs3d_projected_splat* proj, const uint32_t* sorted_keys,
+                               const gs3d_projected_splat* proj, const uint32_t* rect8,
+                               const uint32_t* sorted_keys,
                                const uint32_t* sorted_ids,
                                const uint32_t* sorted_offsets, const uint32_t* ref_counter,
                                uint32_t capacity, uint2* keys, uint32_t* values,
@@ -233,7 +249,7 @@ cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t
 #define GS3D_EMIT_CASE(TP, BINS)                                                              \
   case TP:                                                                                    \
     emit_sorted_kernel<TP, BINS><<<blocks, kThreads, 0, s>>>(                                 \
-        views, n_views, n, proj, sorted_keys, sorted_ids, sorted_offsets, ref_counter,        \
+        views, n_views, n, proj, rect8, sorted_keys, sorted_ids, sorted_offsets, ref_counter, \
         capacity, keys,                                                                       \
         values, sh, mk, g_hist, err);                                                         \
     break;

@@ -222,8 +222,8 @@ __host__ __device__ inline uint32_t digit_mask(int nbits) { return (1u << nbits)
 // degrees and sizes the shared-memory staging).
 cudaError_t launch_preprocess(const ViewDesc* views, uint32_t n_views, uint32_t total_blocks,
                               uint32_t max_sh_degree, gs3d_projected_splat* out, uint32_t* counts,
-                              uint32_t* depth_keys, uint32_t* depth_ids, uint32_t* err,
-                              cudaStream_t s);
+                              uint32_t* depth_keys, uint32_t* depth_ids, uint32_t* rect8,
+                              uint32_t* err, cudaStream_t s);
 // Exclusive scan of counts[gather[i]] (counts[i] when gather is null).
 cudaError_t launch_scan(const uint32_t* counts, const uint32_t* gather, uint32_t* offsets,
                         uint32_t n, unsigned long long* status, uint32_t* tile_counter,
@@ -299,8 +299,11 @@ cudaError_t launch_log_costs(const uint32_t* costs, uint32_t n, float* out, cuda
 
 // Emit in depth-sorted order over all splat-views of a batch (global tile
 // ids, global splat-view values) + histograms of the tile-id digit places.
+// rect8: the preprocess's one-word tile rectangles (null: read the
+// rectangles from the projected records).
 cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t total,
-                               const gs3d_projected_splat* proj, const uint32_t* sorted_keys,
+                               const gs3d_projected_splat* proj, const uint32_t* rect8,
+                               const uint32_t* sorted_keys,
                                const uint32_t* sorted_ids,
                                const uint32_t* sorted_offsets, const uint32_t* ref_counter,
                                uint32_t capacity, uint2* keys, uint32_t* values,

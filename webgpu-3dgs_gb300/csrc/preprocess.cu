@@ -87,6 +87,7 @@ __device__ __forceinline__ void preprocess_block(const ViewDesc* __restrict__ vi
                                                  uint32_t* __restrict__ counts,
                                                  uint32_t* __restrict__ depth_keys,
                                                  uint32_t* __restrict__ depth_ids,
+                                                 uint32_t* __restrict__ rect8,
                                                  uint32_t* __restrict__ err) {
   constexpr int K = (DEG + 1) * (DEG + 1) - 1;
   constexpr int KC = 3 * K;  // floats of SH rest per splat
@@ -274,6 +275,10 @@ __device__ __forceinline__ void preprocess_block(const ViewDesc* __restrict__ vi
       if (depth_keys != nullptr) {  // per-splat depth sort keys of the fused rebin
         depth_keys[gi] = valid ? __float_as_uint(-r0.z) : 0xffffffffu;
         depth_ids[gi] = gi;
+        // tile rectangle in one word [x0, y0, x1 - x0, y1 - y0] (8 bits each;
+        // requested only when every view has at most 256 tiles per axis)
+        if (rect8 != nullptr)
+          rect8[gi] = r3.x | (r3.y << 8) | ((r3.z - r3.x) << 16) | ((r3.w - r3.y) << 24);
       }
     }
   }
@@ -284,6 +289,7 @@ __global__ void __launch_bounds__(kThreads)
     preprocess_kernel(const ViewDesc* __restrict__ views, uint32_t n_views,
                       gs3d_projected_splat* __restrict__ out, uint32_t* __restrict__ counts,
                       uint32_t* __restrict__ depth_keys, uint32_t* __restrict__ depth_ids,
+                      uint32_t* __restrict__ rect8,
                       uint32_t* __restrict__ err) {
   extern __shared__ __align__(16) float s_sh[];
   __shared__ uint64_t s_bar;
@@ -297,22 +303,22 @@ __global__ void __launch_bounds__(kThreads)
   switch (deg) {  // uniform per block
     case 0:
       preprocess_block<0>(views, v, local_first, s_sh, &s_bar, out, counts, depth_keys,
-                          depth_ids, err);
+                          depth_ids, rect8, err);
       break;
     case 1:
       if (MAXDEG >= 1)
         preprocess_block<MAXDEG >= 1 ? 1 : 0>(views, v, local_first, s_sh, &s_bar, out, counts,
-                                              depth_keys, depth_ids, err);
+                                              depth_keys, depth_ids, rect8, err);
       break;
     case 2:
       if (MAXDEG >= 2)
         preprocess_block<MAXDEG >= 2 ? 2 : 0>(views, v, local_first, s_sh, &s_bar, out, counts,
-                                              depth_keys, depth_ids, err);
+                                              depth_keys, depth_ids, rect8, err);
       break;
     default:
       if (MAXDEG >= 3)
         preprocess_block<MAXDEG >= 3 ? 3 : 0>(views, v, local_first, s_sh, &s_bar, out, counts,
-                                              depth_keys, depth_ids, err);
+                                              depth_keys, depth_ids, rect8, err);
       break;
   }
 }
@@ -321,7 +327,8 @@ __global__ void __launch_bounds__(kThreads)
 
 cudaError_t launch_preprocess(const ViewDesc* views, uint32_t n_views, uint32_t total_blocks,
                               uint32_t max_sh_degree, gs3d_projected_splat* out, uint32_t* counts,
-                              uint32_t* depth_keys, uint32_t* depth_ids, uint32_t* err,
+                              uint32_t* depth_keys, uint32_t* depth_ids, uint32_t* rect8,
+                              uint32_t* err,
                               cudaStream_t s) {
   if (total_blocks == 0) return cudaSuccess;
   const uint32_t kc = 3u * ((max_sh_degree + 1) * (max_sh_degree + 1) - 1);
@@ -330,19 +337,19 @@ cudaError_t launch_preprocess(const ViewDesc* views, uint32_t n_views, uint32_t 
   switch (max_sh_degree) {
     case 0:
       preprocess_kernel<0><<<total_blocks, kThreads, 0, s>>>(views, n_views, out, counts,
-                                                             depth_keys, depth_ids, err);
+                                                             depth_keys, depth_ids, rect8, err);
       break;
     case 1:
       preprocess_kernel<1><<<total_blocks, kThreads, smem, s>>>(views, n_views, out, counts,
-                                                                depth_keys, depth_ids, err);
+                                                                depth_keys, depth_ids, rect8, err);
       break;
     case 2:
       preprocess_kernel<2><<<total_blocks, kThreads, smem, s>>>(views, n_views, out, counts,
-                                                                depth_keys, depth_ids, err);
+                                                                depth_keys, depth_ids, rect8, err);
       break;
     default:
       preprocess_kernel<3><<<total_blocks, kThreads, smem, s>>>(views, n_views, out, counts,
-                                                                depth_keys, depth_ids, err);
+                                                                depth_keys, depth_ids, rect8, err);
       break;
   }
   return cudaGetLastError();
