@@ -117,15 +117,56 @@ def make_workload(n_views: int):
     return data, cams
 
 
+def c0_workload():
+    """The small benchmark scene: 100k splats (seed 0), SH 0, one camera at
+    distance 6, 1280x720 (rendered at 16x16 tiles)."""
+    from gs3d import scenes
+    w, h = 1280, 720
+    return scenes.scene_small(100_000, seed=0), \
+        scenes.small_camera(w, h).getUniformData(w, h), (w, h)
+
+
+def cpu_c0_stages(threads):
+    """The oracle's six stages on the small benchmark scene, each timed, at
+    `threads` threads (the scan, emit and identify restatements are serial)."""
+    from oracle import Oracle
+    o = Oracle()
+    data, u, (w, h) = c0_workload()
+    tx, ty = -(-w // TILE), -(-h // TILE)
+    t = {}
+    t0 = time.perf_counter()
+    proj, counts = o.preprocess(u, (tx, ty), (np.float32(1.0 / TILE), np.float32(1.0 / TILE)),
+                                data.positions, data.scales, data.rotations, data.colors,
+                                threads=threads)
+    t1 = time.perf_counter()
+    off, total = o.prefix_scan(counts)
+    t2 = time.perf_counter()
+    keys, vals = o.emit(tx, proj, off, total)
+    t3 = time.perf_counter()
+    keys, vals = o.radix_sort(keys, vals, threads)
+    t4 = time.perf_counter()
+    toff = o.identify(keys, tx * ty)
+    t5 = time.perf_counter()
+    o.rasterize(w, h, TILE, TILE, proj, toff, vals, threads)
+    t6 = time.perf_counter()
+    t = {"preprocess-splats": t1 - t0, "prefix-scan": t2 - t1, "emit-tile-refs": t3 - t2,
+         "radix-sort": t4 - t3, "identify-tile-ranges": t5 - t4, "rasterize-tiles": t6 - t5}
+    total_s = t6 - t0
+    return {"views_per_s": round(1.0 / total_s, 2), "threads": threads,
+            "stage_ms": {k: round(v * 1e3, 2) for k, v in t.items()}}
+
+
 def algorithmic_bytes(n, R, tiles, tile_passes, sh_floats, fused):
     """Minimum bytes each stage must move for one view (inputs read once,
     outputs written once), the numerator of the per-stage roofline."""
     full_passes = 4 + tile_passes
     return {
-        "preprocess-splats": n * (64 + 4 * sh_floats) + n * (64 + 4 + (8 if fused else 0)),
+        # fused: + depth key, depth id and the one-word tile rectangle per splat-view
+        "preprocess-splats": n * (64 + 4 * sh_floats) + n * (64 + 4 + (12 if fused else 0)),
         "depth-sort": 4 * n + 4 * 16 * n,
         "prefix-scan": 12 * n if fused else 8 * n,
-        "emit-tile-refs": n * (4 + 24 + 4) + 12 * R if fused else n * (24 + 4) + 12 * R,
+        # fused: depth id, depth key, offset and one-word rectangle per splat-view
+        "emit-tile-refs": n * (4 + 4 + 4 + 4) + 12 * R if fused else n * (24 + 4) + 12 * R,
         "radix-sort": tile_passes * 24 * R if fused else 8 * R + full_passes * 24 * R,
         "identify-tile-ranges": 4 * R + 4 * (tiles + 1),
         "rasterize-tiles": 44 * R + 8 * WIDTH * HEIGHT,
@@ -134,20 +175,21 @@ def algorithmic_bytes(n, R, tiles, tile_passes, sh_floats, fused):
 
 # DRAM bytes per unit of the HBM-bound kernels, from ncu captures of a
 # 2-view batch of the same workload (profiles/), scaled to a launch by the
-# units it processes: tile-digit pass per ref (32x32 / 16x16 tiles),
-# preprocess per splat-view, emit per (splat-view, ref).
+# units it processes: tile-digit pass per ref (32x32 / 16x16 tiles);
+# preprocess per scene splat read + per splat-view written; emit per
+# (splat-view, ref) at 32x32 tiles with one-word rectangles.
 DRAM_PER_REF_PASS = {32: 22.6, 16: 25.1}
-DRAM_PREPROCESS_PER_SPLAT = 1894.3e6 / 6e6
-DRAM_EMIT = {32: (1034.6e6, 6e6, 23.7e6), 16: (1484.9e6, 6e6, 57.2e6)}
+DRAM_PREPROCESS = (732.1e6 / 3e6, 434.7e6 / 6e6)
+DRAM_EMIT = {32: (365.2e6, 6e6, 23.7e6)}
 
 
-def dominant_traffic(stage, tile, refs_per_launch, splats_per_launch):
+def dominant_traffic(stage, tile, refs_per_launch, splats_per_launch, scene_splats):
     """Measured DRAM bytes of one launch of the dominant HBM-bound kernel, or
     None where no capture covers it."""
     if stage == "radix-sort" and tile in DRAM_PER_REF_PASS:
         return int(DRAM_PER_REF_PASS[tile] * refs_per_launch)
     if stage == "preprocess-splats":
-        return int(DRAM_PREPROCESS_PER_SPLAT * splats_per_launch)
+        return int(DRAM_PREPROCESS[0] * scene_splats + DRAM_PREPROCESS[1] * splats_per_launch)
     if stage == "emit-tile-refs" and tile in DRAM_EMIT:
         b, n, r = DRAM_EMIT[tile]
         return int(b * (0.5 * splats_per_launch / n + 0.5 * refs_per_launch / r))
@@ -302,6 +344,27 @@ def run_ours(args, rank, world):
     views = args.steps * len(cam_structs)
     # headline: batched, autotuned, learned schedule, CUDA graph replays
     batched_ms, _, clocks = timed("batched", batched_schedule, graph=True)
+    # the same path, each batch bracketed by its own events: the median over
+    # steps x batches samples (the reference's timing protocol)
+    check(lib.gs3d_set_flags(ctx, _lib.FLAG_CUDA_GRAPH))
+    check(lib.gs3d_set_schedule(ctx, batched_schedule))
+    run_step("batched")
+    check(lib.gs3d_synchronize(ctx))
+    marks = []
+    for _ in range(max(args.steps, 3)):
+        for arr in batches:
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[0].record(stream)
+            check(lib.gs3d_rebin_batch(ctx, C.cast(arr, C.c_void_p), len(arr)))
+            ev[1].record(stream)
+            marks.append((ev, len(arr)))
+    check(lib.gs3d_synchronize(ctx))
+    torch.cuda.synchronize()
+    per_view_ms = sorted(a.elapsed_time(b) / n for (a, b), n in marks)
+    batch_median = {"ms_per_view": round(statistics.median(per_view_ms), 4),
+                    "views_per_s": round(1e3 / statistics.median(per_view_ms), 1),
+                    "samples": len(per_view_ms)}
+    check(lib.gs3d_set_flags(ctx, 0))
     eager_ms, batched_stages, _ = timed("batched", batched_schedule)  # per-stage events
     # the raster under each work order on the tuned batched path (same image)
     sched_batched = {}
@@ -351,6 +414,35 @@ def run_ours(args, rank, world):
         ms_, st_, _ = timed("fused", sc)
         sched_raster[name] = {"raster_ms": round(st_["rasterize-tiles"][0], 4),
                               "views_per_s": round(views * world / (ms_ * 1e-3), 1)}
+
+    # the small benchmark scene (100k splats, SH 0, 1280x720, 16x16 tiles):
+    # single-view fused rebins replayed as a graph, beside the CPU C0 figures
+    c0_data, c0_u, (c0_w, c0_h) = c0_workload()
+    check(lib.gs3d_set_splats(ctx, c0_data.splatCount, ptr(c0_data.positions),
+                              ptr(c0_data.scales), ptr(c0_data.rotations),
+                              ptr(c0_data.colors), None, 0, 0))
+    c0_cam = camera_struct(c0_u)
+    check(lib.gs3d_set_flags(ctx, _lib.FLAG_CUDA_GRAPH))
+    check(lib.gs3d_set_schedule(ctx, _lib.SCHEDULE_ROW_MAJOR))
+    for _ in range(3):
+        rc = lib.gs3d_rebin(ctx, C.byref(c0_cam), c0_w, c0_h)
+        rc = lib.gs3d_synchronize(ctx) if rc == 0 else rc
+        if rc != _lib.ERR_CAPACITY:
+            check(rc)
+            break
+    c0_reps = 200
+    for _ in range(20):
+        check(lib.gs3d_rebin(ctx, C.byref(c0_cam), c0_w, c0_h))
+    check(lib.gs3d_synchronize(ctx))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(c0_reps):
+        check(lib.gs3d_rebin(ctx, C.byref(c0_cam), c0_w, c0_h))
+    e1.record(stream)
+    check(lib.gs3d_synchronize(ctx))
+    torch.cuda.synchronize()
+    c0_gpu = round(c0_reps / (e0.elapsed_time(e1) * 1e-3), 1)
+    check(lib.gs3d_set_flags(ctx, 0))
     lib.gs3d_destroy(ctx)
 
     tiles16 = -(-WIDTH // TILE) * -(-HEIGHT // TILE)
@@ -397,8 +489,15 @@ def run_ours(args, rank, world):
         "tuning": {"tile": tuned.tile_w, "digit_bits": tuned.digit_bits,
                    "raster_batch": tuned.raster_batch, "candidates": tune_table},
         "tile_passes_batched": tuned_passes,
-        "traffic": dominant_traffic(dom, tuned.tile_w, tuned_R * B, N_SPLATS * B),
+        "traffic": dominant_traffic(dom, tuned.tile_w, tuned_R * B, N_SPLATS * B, N_SPLATS),
         "launch_units": {"refs": int(tuned_R * B), "splat_views": N_SPLATS * B},
+        "batch_median": batch_median, "c0_gpu_views_per_s": c0_gpu,
+        # bytes the sort moves per view: the reference's eight 8-bit passes over
+        # 12-byte refs at its 16x16 tiles (one histogram read + 8 scatters)
+        # against this path's 4 depth passes over splats + its tile-digit passes
+        "sort_bytes_per_view": {
+            "reference_8_pass_16x16": int(8 * mean_R + 8 * 24 * mean_R),
+            "this_path": int(4 * N_SPLATS + 4 * 16 * N_SPLATS + tuned_passes * 24 * tuned_R)},
     }
 
 
@@ -501,8 +600,13 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         times, threads = cpu_view_seconds(1)
+        from oracle import Oracle
         cpu = {"value": 1.0 / times[0], "unit": "views/s", "cores": threads, "kind": "port",
-               "sample": "one full 3M-splat SH3 1080p view (orbit pose 0), oracle rebin"}
+               "sample": "one full 3M-splat SH3 1080p view (orbit pose 0), oracle rebin",
+               "c0_100k_720p": {"threads_1": cpu_c0_stages(1),
+                                f"threads_{Oracle().max_threads()}":
+                                    cpu_c0_stages(Oracle().max_threads()),
+                                "gpu_single_view_fused_views_per_s": res["c0_gpu_views_per_s"]}}
     if rank == 0:
         dom = res["per_stage"][res["dominant"]]
         out = {
@@ -525,7 +629,9 @@ def main():
                        "schedules_single_view": res["schedules"],
                        "schedules_batched_tuned": res["schedules_batched"],
                        "cost_model_heldout": res["cost_model"],
-                       "plain_stagewise_views_per_s": res["stagewise_value"]},
+                       "plain_stagewise_views_per_s": res["stagewise_value"],
+                       "batch_median": res["batch_median"],
+                       "sort_bytes_per_view": res["sort_bytes_per_view"]},
             "roofline": {"bound": "hbm", "kernel": res["dominant"], "achieved": dom["gbs"],
                          "peak": res["peak"], "unit": "GB/s", "frac": dom["frac_hbm"],
                          "peak_kind": res["peak_kind"], "traffic": res["traffic"],
