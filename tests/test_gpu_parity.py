@@ -108,7 +108,9 @@ def test_sh_colour_degrees(renderer, oracle, deg):
 
 
 @pytest.mark.parametrize("w,h,tw,th", [(1000, 563, 16, 16), (640, 360, 8, 8), (1024, 600, 32, 32),
-                                       (333, 217, 12, 20), (17, 9, 16, 16), (4000, 40, 4, 4)])
+                                       (333, 217, 12, 20), (17, 9, 16, 16), (4000, 40, 4, 4),
+                                       # 1024-pixel tiles shaded by one, two or four strip CTAs
+                                       (1000, 563, 128, 8), (900, 500, 64, 16), (700, 450, 16, 64)])
 @pytest.mark.parametrize("stagewise", [False, True])
 def test_ragged_viewports_and_tile_sizes(renderer, oracle, w, h, tw, th, stagewise):
     data = scenes.scene_small(40_000, seed=5)
