@@ -108,13 +108,33 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_workload(n_views: int):
+def make_workload(n_views: int, rank: int = 0):
+    """The 3M-splat scene and `n_views` orbit cameras.  Every rank renders the
+    same scene from its own poses (elevation jitter seeded by the rank), so
+    ranks hold disjoint views and rank 0's are the single-GPU workload."""
     from gs3d import scenes
     data = scenes.scene_clusters(N_SPLATS, seed=0, sh_degree=3)
-    eyes = scenes.orbit_eyes(64, radius=12.0, jitter_deg=20.0, seed=0)
-    cams = [scenes.camera_at(eyes[i % 64], WIDTH, HEIGHT).getUniformData(WIDTH, HEIGHT)
+    return data, workload_cameras(n_views, rank)
+
+
+def workload_cameras(n_views: int, rank: int = 0):
+    """Camera uniforms of `rank`'s views: the 64-pose orbit (radius 12,
+    +-20 deg elevation jitter seeded by the rank), repeated to `n_views`."""
+    from gs3d import scenes
+    eyes = scenes.orbit_eyes(64, radius=12.0, jitter_deg=20.0, seed=rank)
+    return [scenes.camera_at(eyes[i % 64], WIDTH, HEIGHT).getUniformData(WIDTH, HEIGHT)
             for i in range(n_views)]
-    return data, cams
+
+
+def max_over_ranks(value: float, world: int, device: str = "cuda") -> float:
+    """The largest of every rank's `value` (the slowest rank's time), on all
+    ranks; the identity for a single process."""
+    if world <= 1:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
 
 
 def c0_workload():
@@ -235,7 +255,7 @@ def run_ours(args, rank, world):
         if rc != 0:
             raise RuntimeError(lib.gs3d_last_error(ctx).decode())
 
-    data, cams = make_workload(args.views)
+    data, cams = make_workload(args.views, rank)
     ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
     check(lib.gs3d_set_splats(ctx, data.splatCount, ptr(data.positions), ptr(data.scales),
                               ptr(data.rotations), ptr(data.colors),
@@ -331,11 +351,7 @@ def run_ours(args, rank, world):
         check(lib.gs3d_read_stage_times(ctx, ms, cnt))
         check(lib.gs3d_set_flags(ctx, 0))
         check(lib.gs3d_set_schedule(ctx, _lib.SCHEDULE_ROW_MAJOR))
-        total = start.elapsed_time(stop)
-        if world > 1:
-            t = torch.tensor([total], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total = float(t.item())
+        total = max_over_ranks(start.elapsed_time(stop), world)
         views = args.steps * len(cam_structs)
         per_stage = {name: (ms[i] / views, cnt[i] / views) for i, name in
                      enumerate(_lib.STAGE_NAMES) if cnt[i]}  # per view
@@ -388,6 +404,8 @@ def run_ours(args, rank, world):
                 ctx, 14, C.c_void_p(pinned.data_ptr() + (bi % 2) * batch_bytes),
                 img_bytes * len(arr)))
     check(lib.gs3d_synchronize(ctx))
+    if world > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -401,8 +419,8 @@ def run_ours(args, rank, world):
                 img_bytes * len(arr)))
     e1.record(stream)
     check(lib.gs3d_synchronize(ctx))
-    e2e_wall = time.perf_counter() - t0
-    e2e_ms = e0.elapsed_time(e1)
+    e2e_wall = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), world)
     check(lib.gs3d_set_flags(ctx, 0))
 
     # ---- reference tuning (16x16 tiles, 8-bit digits, one splat per pixel
@@ -484,7 +502,7 @@ def run_ours(args, rank, world):
         "stagewise_stages": roof(stagewise_stages, False, mean_R, tiles16, tile_passes16, TILE),
         # the image copy-outs run on the library's copy stream: the host clock
         # around the loop, which ends in gs3d_synchronize, covers all of them
-        "e2e_value": views * world / e2e_wall, "e2e_stream_value": views / (e2e_ms * 1e-3),
+        "e2e_value": views * world / e2e_wall, "e2e_stream_value": views * world / (e2e_ms * 1e-3),
         "h2d": 416 * len(cam_structs), "d2h": img_bytes * len(cam_structs),
         "launches_per_step": launches_per_batch * len(batches),
         "schedules": sched_raster, "schedules_batched": sched_batched,
