@@ -1,5 +1,5 @@
-"""CPU restatement of the render passes after the rasterizer, the checker of
-gs3d_composite.  TEST INFRASTRUCTURE ONLY.
+"""CPU restatement of the render passes after the rasterizer, which the tests
+compare gs3d_composite with.  TEST INFRASTRUCTURE ONLY.
 
   * debug_tile_overlay.wgsl main_fs (src/shaders/render/debug_tile_overlay.wgsl
     :37-60): tile = min(px / tile_size, tile_count - 1); count = hi - lo

@@ -1,7 +1,7 @@
 // gs_oracle.cpp - CPU restatement of the webgpu-3dgs per-frame rebin path.
 //
-// TEST INFRASTRUCTURE ONLY: the checker for the CUDA library and the timed CPU
-// baseline.  Nothing in the library links or loads this file.
+// TEST INFRASTRUCTURE ONLY: what the tests compare the CUDA library with, and
+// the timed CPU baseline.  Nothing in the library links or loads this file.
 //
 // Parity status: UNPINNED against executable reference output (the reference
 // is WGSL that needs a WebGPU implementation, unavailable here, and it ships

@@ -1,8 +1,8 @@
 /*
  * gs_oracle.h - CPU restatement of the webgpu-3dgs rebin path.
  *
- * TEST INFRASTRUCTURE ONLY.  This code is the checker for the CUDA library and
- * the timed CPU baseline; it is never linked into, loaded by, or called from
+ * TEST INFRASTRUCTURE ONLY.  The tests compare the CUDA library with this code,
+ * and it is the timed CPU baseline; it is never linked into, loaded by, or called from
  * the library's product path.
  *
  * Parity status: UNPINNED against executable reference output.  The reference

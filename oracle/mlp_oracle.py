@@ -1,6 +1,6 @@
 """Float64 reference of the cost MLP (16 -> 64 -> 64 -> 1, ReLU) and of the
-gradient of mean((y - t)^2) - TEST INFRASTRUCTURE ONLY: the checker for the
-library's gs3d_mlp_forward / gs3d_mlp_backward / gs3d_mlp_infer kernels.
+gradient of mean((y - t)^2) - TEST INFRASTRUCTURE ONLY: the tests compare the
+library's gs3d_mlp_forward / gs3d_mlp_backward / gs3d_mlp_infer kernels with it.
 The layout of the parameter vector is the library's:
 W1[64][16] | b1[64] | W2[64][64] | b2[64] | w3[64] | b3."""
 from __future__ import annotations

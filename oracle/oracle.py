@@ -1,7 +1,7 @@
 """ctypes bindings of liboracle.so (CPU restatement of the rebin path).
 
-TEST INFRASTRUCTURE ONLY: the checker for the CUDA library and the timed CPU
-baseline.  Every array crossing the boundary is a C-contiguous numpy array in
+TEST INFRASTRUCTURE ONLY: what the tests compare the CUDA library with, and the
+timed CPU baseline.  Every array crossing the boundary is a C-contiguous numpy array in
 the reference's layout (vec4 f32 splat SoA, 64-byte ProjectedSplat,
 interleaved u32 [hi, lo] keys).
 """

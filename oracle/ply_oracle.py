@@ -1,6 +1,6 @@
 """CPU restatement of the reference's Gaussian-splat PLY loader
-(src/workers/SceneWorker.ts:146-550), the checker of gs3d_ply_inspect and
-gs3d_load_ply.  TEST INFRASTRUCTURE ONLY.
+(src/workers/SceneWorker.ts:146-550), which the tests compare
+gs3d_ply_inspect and gs3d_load_ply with.  TEST INFRASTRUCTURE ONLY.
 
 Follows the reference step by step: the header is read from the first MB up
 to end_header (parsePlyHeader, :149-253), the 14 required vertex properties
