@@ -36,10 +36,12 @@ namespace gs3d {
 namespace {
 
 constexpr int kThreads = 256;   // histogram kernel
-constexpr int kPassThreads = 512;                  // onesweep pass
+constexpr int kPassThreads = 512;                  // onesweep pass (8-bit and narrower digits)
 constexpr int kWarps = kPassThreads / 32;          // 16
 constexpr int kItems = 8;
 constexpr uint32_t kPart = kPassThreads * kItems;  // 4096 keys per partition
+// key buffers are padded to whole partitions of every pass kernel
+constexpr uint32_t kRoundPart = 4096;
 constexpr uint32_t kFlagAgg = 1u, kFlagInc = 2u;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
 constexpr int kLookback = 16;  // predecessor status words fetched per look-back step
@@ -189,7 +191,7 @@ __device__ __forceinline__ uint32_t scan8_inclusive(uint32_t x, int lane) {
 //   C  the partition is reordered by digit and each digit's global
 //      destination is resolved.
 template <typename K, int NBITS>
-__global__ void __launch_bounds__(kPassThreads, 2)
+__global__ void __launch_bounds__(kPassThreads, 1024 / kPassThreads)
     onesweep_kernel(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                     K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                     const uint32_t* __restrict__ ref_counter, uint32_t capacity, int word,
@@ -204,6 +206,10 @@ __global__ void __launch_bounds__(kPassThreads, 2)
   __shared__ uint32_t s_part[2];  // partition id of each buffer
   __shared__ uint64_t s_bar[2];
 
+  if (blockDim.x != kPassThreads) {  // the indexing below is written for this block size
+    if (threadIdx.x == 0) latch_error(err, DEVERR_RANGE);
+    return;
+  }
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t R = live_refs(ref_counter, capacity);
   const uint32_t num_parts = (R + kPart - 1) / kPart;
@@ -373,9 +379,8 @@ __global__ void __launch_bounds__(kPassThreads, 2)
       break;  // no fetch is in flight: the next claim comes after this barrier
     }
     // the other buffer's last readers (previous write-out) passed barrier A;
-    // a thread without a digit claims, so the digit warps' write-out is not
-    // held up by the claim's round trip
-    if (tid == kRadixBins) claim_into(b ^ 1);
+    // the last thread claims (with more than 256 threads it owns no digit)
+    if (tid == kPassThreads - 1) claim_into(b ^ 1);
     // ---- write each digit run contiguously ----
     for (uint32_t j = tid; j < count; j += kPassThreads) {
       const K k = s_keys[j];
@@ -396,13 +401,17 @@ __global__ void __launch_bounds__(kPassThreads, 2)
 // per-warp counts take 64 KB, so one CTA runs per SM; every thread owns four
 // consecutive digits for the per-digit work and the look-back.
 constexpr int kWideBits = 11;
+constexpr int kWideThreads = 512;
+constexpr int kWideWarps = kWideThreads / 32;         // 16
+constexpr uint32_t kWidePart = kWideThreads * kItems;  // 4096 keys per partition
+constexpr size_t wide_buf_bytes() { return (size_t)kWidePart * (sizeof(uint2) + sizeof(uint32_t)); }
 constexpr uint32_t kWideBins = 1u << kWideBits;
-constexpr uint32_t kWideDigitsPerThread = kWideBins / kPassThreads;  // 4
+constexpr uint32_t kWideDigitsPerThread = kWideBins / kWideThreads;  // 4
 constexpr int kWideLookback = 8;
 
 template <typename K>
 constexpr size_t wide_pass_smem() {
-  return 2 * part_buf_bytes<K>() + (size_t)kWarps * kWideBins * sizeof(uint16_t) +
+  return 2 * wide_buf_bytes() + (size_t)kWideWarps * kWideBins * sizeof(uint16_t) +
          3 * (size_t)kWideBins * sizeof(uint32_t);
 }
 
@@ -420,7 +429,7 @@ __device__ __forceinline__ uint32_t scan16_inclusive(uint32_t x, int lane) {
   return x;
 }
 
-__global__ void __launch_bounds__(kPassThreads, 1)
+__global__ void __launch_bounds__(kWideThreads, 1)
     onesweep_wide_kernel(const uint2* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                          uint2* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                          const uint32_t* __restrict__ ref_counter, uint32_t capacity, int word,
@@ -428,18 +437,22 @@ __global__ void __launch_bounds__(kPassThreads, 1)
                          uint32_t* __restrict__ status, uint32_t* __restrict__ part_counter,
                          uint32_t* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
-  constexpr size_t kBuf = part_buf_bytes<uint2>();
-  uint16_t* s_whist = reinterpret_cast<uint16_t*>(smem + 2 * kBuf);  // [kWarps][2048]
-  uint32_t* s_bucket = reinterpret_cast<uint32_t*>(smem + 2 * kBuf + kWarps * kWideBins * 2);
+  constexpr size_t kBuf = wide_buf_bytes();
+  uint16_t* s_whist = reinterpret_cast<uint16_t*>(smem + 2 * kBuf);  // [kWideWarps][2048]
+  uint32_t* s_bucket = reinterpret_cast<uint32_t*>(smem + 2 * kBuf + kWideWarps * kWideBins * 2);
   uint32_t* s_dloc = s_bucket + kWideBins;  // exclusive start within the digit warp
   uint32_t* s_dest = s_dloc + kWideBins;
-  __shared__ uint32_t s_wsum[kWarps];
+  __shared__ uint32_t s_wsum[kWideWarps];
   __shared__ uint32_t s_part[2];
   __shared__ uint64_t s_bar[2];
 
+  if (blockDim.x != kWideThreads) {  // the indexing below is written for this block size
+    if (threadIdx.x == 0) latch_error(err, DEVERR_RANGE);
+    return;
+  }
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t R = live_refs(ref_counter, capacity);
-  const uint32_t num_parts = (R + kPart - 1) / kPart;
+  const uint32_t num_parts = (R + kWidePart - 1) / kWidePart;
   constexpr uint32_t kDigitMask = kWideBins - 1u;
   const uint32_t d0 = tid * kWideDigitsPerThread;  // this thread's digits d0 .. d0+3
 
@@ -448,11 +461,11 @@ __global__ void __launch_bounds__(kPassThreads, 1)
     s_part[b] = part;
     if (part < num_parts) {
       unsigned char* buf = smem + b * kBuf;
-      const uint32_t kb = kPart * sizeof(uint2), vb = kPart * sizeof(uint32_t);
+      const uint32_t kb = kWidePart * sizeof(uint2), vb = kWidePart * sizeof(uint32_t);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_expect_tx(&s_bar[b], kb + vb);
-      bulk_g2s(buf, keys_in + (size_t)part * kPart, kb, &s_bar[b]);
-      bulk_g2s(buf + kb, vals_in + (size_t)part * kPart, vb, &s_bar[b]);
+      bulk_g2s(buf, keys_in + (size_t)part * kWidePart, kb, &s_bar[b]);
+      bulk_g2s(buf + kb, vals_in + (size_t)part * kWidePart, vb, &s_bar[b]);
     } else {
       mbar_arrive(&s_bar[b]);
     }
@@ -475,7 +488,7 @@ __global__ void __launch_bounds__(kPassThreads, 1)
     const uint32_t inc = warp_inclusive(t, lane);
     if (lane == 31) s_wsum[warp] = inc;
     __syncthreads();
-    const uint32_t wv = lane < kWarps ? s_wsum[lane] : 0u;
+    const uint32_t wv = lane < kWideWarps ? s_wsum[lane] : 0u;
     const uint32_t wex = scan16_inclusive(wv, lane) - wv;
     uint32_t run = __shfl_sync(0xffffffffu, wex, warp) + inc - t;
 #pragma unroll
@@ -496,11 +509,11 @@ __global__ void __launch_bounds__(kPassThreads, 1)
       reinterpret_cast<uint4*>(wh)[lane + 32 * k] = make_uint4(0u, 0u, 0u, 0u);
     __syncwarp();
     uint2* s_keys = reinterpret_cast<uint2*>(smem + b * kBuf);
-    uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + b * kBuf + kPart * sizeof(uint2));
+    uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + b * kBuf + kWidePart * sizeof(uint2));
     const bool landed = mbar_wait(&s_bar[b], b ? phase1 : phase0);
     if (b) phase1 ^= 1u; else phase0 ^= 1u;
     const uint32_t part = landed ? s_part[b] : num_parts;
-    const uint32_t count = part < num_parts ? min(kPart, R - part * kPart) : 0u;
+    const uint32_t count = part < num_parts ? min(kWidePart, R - part * kWidePart) : 0u;
 
     uint2 key[kItems];
     uint32_t val[kItems];
@@ -545,13 +558,13 @@ __global__ void __launch_bounds__(kPassThreads, 1)
       const uint32_t d = d0 + k;
       uint32_t r = 0;
 #pragma unroll
-      for (int w = 0; w < kWarps; ++w) {
+      for (int w = 0; w < kWideWarps; ++w) {
         const uint32_t c = s_whist[w * kWideBins + d];
         s_whist[w * kWideBins + d] = (uint16_t)r;
         r += c;
       }
       run[k] = r;
-      pub[k] = (d == kDigitMask) ? r - (kPart - count) : r;
+      pub[k] = (d == kDigitMask) ? r - (kWidePart - count) : r;
       st_relaxed_u32(status + (size_t)part * kWideBins + d,
                      ((part == 0 ? kFlagInc : kFlagAgg) << 30) | pub[k]);
       t += r;
@@ -568,7 +581,7 @@ __global__ void __launch_bounds__(kPassThreads, 1)
     }
     __syncthreads();  // B
 
-    const uint32_t wv = lane < kWarps ? s_wsum[lane] : 0u;
+    const uint32_t wv = lane < kWideWarps ? s_wsum[lane] : 0u;
     const uint32_t wex = scan16_inclusive(wv, lane) - wv;
 
     // ---- reorder the partition in place ----
@@ -631,8 +644,8 @@ __global__ void __launch_bounds__(kPassThreads, 1)
       if (tid == 0) latch_error(err, DEVERR_TIMEOUT);
       break;
     }
-    if (tid == kPassThreads - 1) claim_into(b ^ 1);
-    for (uint32_t j = tid; j < count; j += kPassThreads) {
+    if (tid == kWideThreads - 1) claim_into(b ^ 1);
+    for (uint32_t j = tid; j < count; j += kWideThreads) {
       const uint2 k = s_keys[j];
       const uint32_t dst = s_dest[wide_digit(k, word, shift)] + j;
       if (dst < R) {
@@ -697,7 +710,7 @@ cudaError_t launch_pass(int nbits, const K* kin, const uint32_t* vin, K* kout, u
     if constexpr (std::is_same<K, uint2>::value) {
       e = onesweep_wide_setup();
       if (e != cudaSuccess) return e;
-      onesweep_wide_kernel<<<(int)std::min<size_t>((size_t)sm_count, parts_cap), kPassThreads,
+      onesweep_wide_kernel<<<(int)std::min<size_t>((size_t)sm_count, parts_cap), kWideThreads,
                              wide_pass_smem<uint2>(), s>>>(kin, vin, kout, vout, ref_counter,
                                                            capacity, word, shift, hist, status,
                                                            part_counter, err);
@@ -816,7 +829,7 @@ SortPlan make_sort_plan(uint32_t num_tiles, int tile_digit_bits) {
 }
 
 uint32_t sort_capacity_round(uint32_t capacity) {
-  return (uint32_t)(((uint64_t)capacity + kPart - 1) / kPart * kPart);
+  return (uint32_t)(((uint64_t)capacity + kRoundPart - 1) / kRoundPart * kRoundPart);
 }
 
 size_t sort_status_words(uint32_t capacity, int passes) {
