@@ -206,16 +206,23 @@ __device__ __forceinline__ bool rect_may_hit(const SplatStage& s, float xlo, flo
   if (ex == 0.0f && ey == 0.0f) return true;  // the mean lies inside
   if (vis == __int_as_float(0x7f800000)) return true;
   const float qa = b.x, qb = b.y, qc = b.z;
-  auto Q = [&](float x, float y) { return fmaf(qa * x, x, fmaf(qb * x, y, qc * y * y)); };
   // edge stationary points, by the fast reciprocal division: an error d in
   // the point raises Q there by qa d^2 (qc d^2) over the edge minimum, far
   // inside the margins folded into vis
   const float sy = __fdividef(-qb, 2.0f * qc), sx = __fdividef(-qb, 2.0f * qa);
-  float m = Q(x0, fminf(fmaxf(sy * x0, y0), y1));
-  m = fminf(m, Q(x1, fminf(fmaxf(sy * x1, y0), y1)));
-  m = fminf(m, Q(fminf(fmaxf(sx * y0, x0), x1), y0));
-  m = fminf(m, Q(fminf(fmaxf(sx * y1, x0), x1), y1));
-  return m <= vis;
+  // Q = qa x^2 + qb x y + qc y^2 at the two vertical edges (x0, x1 at their
+  // clamped stationary y) and the two horizontal ones, as pairs
+  const float2 vx = make_float2(x0, x1), hy = make_float2(y0, y1);
+  const float2 svy = __fmul2_rn(bcast(sy), vx), shx = __fmul2_rn(bcast(sx), hy);
+  const float2 vy = make_float2(fminf(fmaxf(svy.x, y0), y1), fminf(fmaxf(svy.y, y0), y1));
+  const float2 hx = make_float2(fminf(fmaxf(shx.x, x0), x1), fminf(fmaxf(shx.y, x0), x1));
+  auto Q2 = [&](float2 x, float2 y) {
+    return __ffma2_rn(__fmul2_rn(bcast(qa), x), x,
+                      __ffma2_rn(__fmul2_rn(bcast(qb), x), y,
+                                 __fmul2_rn(__fmul2_rn(bcast(qc), y), y)));
+  };
+  const float2 qv = Q2(vx, vy), qh = Q2(hx, hy);
+  return fminf(fminf(qv.x, qv.y), fminf(qh.x, qh.y)) <= vis;
 }
 
 struct TileGeom {
