@@ -99,9 +99,10 @@ __global__ void __launch_bounds__(kThreads)
                        uint2* __restrict__ keys, uint32_t* __restrict__ values, int4 shifts,
                        uint4 masks, uint32_t* __restrict__ g_hist, uint32_t* __restrict__ err) {
   __shared__ uint32_t s_off[kThreads + 1];
-  __shared__ uint32_t s_tminx[kThreads], s_tminy[kThreads], s_w[kThreads], s_cnt[kThreads];
-  __shared__ uint32_t s_lo[kThreads], s_id[kThreads], s_tx[kThreads], s_tb[kThreads];
-  __shared__ float s_winv[kThreads];
+  // per splat, read as two 16-byte words by every ref it owns:
+  // [count, rectangle width, bits(1/width), tiles_x - width] and
+  // [global tile of the rectangle's first tile, depth bits, splat-view id, -]
+  __shared__ uint4 s_ra[kThreads], s_rb[kThreads];
   __shared__ uint32_t s_hist[TP > 0 ? TP : 1][BINS];
 
   const uint32_t total = *ref_counter;
@@ -136,15 +137,12 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t v =
         find_view(n_views, id, [&](uint32_t k) { return __ldg(&views[k].splat_base); });
     s_off[threadIdx.x] = __ldg(sorted_offsets + i);
-    s_tminx[threadIdx.x] = x0;
-    s_tminy[threadIdx.x] = y0;
-    s_w[threadIdx.x] = w;
-    s_cnt[threadIdx.x] = w * h;
-    s_lo[threadIdx.x] = __ldg(sorted_keys + i);
-    s_id[threadIdx.x] = id;
-    s_tx[threadIdx.x] = __ldg(&views[v].f.tile_count[0]);
-    s_tb[threadIdx.x] = __ldg(&views[v].f.tile_base);
-    s_winv[threadIdx.x] = 1.0f / (float)w;
+    const uint32_t tx = __ldg(&views[v].f.tile_count[0]);
+    // ref k of the splat: row = k / w, tile = first + row * tx + (k - row * w)
+    //                                      = first + row * (tx - w) + k
+    s_ra[threadIdx.x] = make_uint4(w * h, w, __float_as_uint(1.0f / (float)w), tx - w);
+    s_rb[threadIdx.x] = make_uint4(__ldg(&views[v].f.tile_base) + y0 * tx + x0,
+                                   __ldg(sorted_keys + i), id, 0u);
   }
   const uint32_t last = min(n, first + kThreads);
   if (threadIdx.x == 0) s_off[last - first] = __ldg(sorted_offsets + last);
@@ -202,14 +200,15 @@ __global__ void __launch_bounds__(kThreads)
     uint32_t tile = 0;
     if (live) {
       const uint32_t k = j - s_off[o];
-      if (k < s_cnt[o]) {
+      const uint4 ra = s_ra[o];
+      if (k < ra.x) {
         // row = floor(k / w) by a float reciprocal: exact while k + w < 2^22
         // (k < w * h <= tiles of one view)
-        const uint32_t w = s_w[o];
-        const uint32_t row = (uint32_t)(((float)k + 0.5f) * s_winv[o]);
-        tile = s_tb[o] + (s_tminy[o] + row) * s_tx[o] + s_tminx[o] + (k - row * w);
-        keys[j] = make_uint2(tile, s_lo[o]);
-        values[j] = s_id[o];
+        const uint32_t row = (uint32_t)(((float)k + 0.5f) * __uint_as_float(ra.z));
+        const uint4 rb = s_rb[o];
+        tile = rb.x + row * ra.w + k;
+        keys[j] = make_uint2(tile, rb.y);
+        values[j] = rb.z;
       } else {
         live = false;
       }
