@@ -23,19 +23,22 @@
 //    whose sides divide by 8 and 4) and tests every staged splat once against
 //    it; a splat is skipped for the whole warp only when no pixel centre of
 //    the block can pass the per-pixel tests: the block lies outside the
-//    radius circle, or the exact minimum of d^T conic d over the block keeps
-//    alpha below 1/255, with margins that cover f32 rounding.  Pixels
-//    therefore blend exactly the same splats in the same order, and the
-//    image is bit-identical to the one-thread-per-pixel variant;
+//    radius circle, or the minimum of d^T conic d over the block keeps
+//    alpha below 1/255, with margins that cover f32 rounding and the fast
+//    division of the edge minimisers.  Pixels therefore blend exactly the
+//    same splats in the same order, and the image is bit-identical to the
+//    one-thread-per-pixel variant;
 //  * (two-pixel variant, tiles whose sides divide by 8) each warp owns an 8x8
 //    block, a lane shading rows y and y + 4 of one column with the paired
 //    FP32 instructions of sm_100 (each half rounded like the scalar path);
-//    tiles above 512 pixels are shaded by several CTAs, one row strip each;
+//    tiles above 512 pixels are shaded by four (else two) CTAs, one row
+//    strip each, whose tile costs combine by maximum;
 //  * each CTA records the tile's cost: the number of splats iterated before
 //    its last pixel terminated.
 //
-// Both variants call the same per-pixel function, so they compile to the same
-// arithmetic.  Against the reference's f32 expression order the per-pixel
+// The variants share the per-pixel arithmetic (the two-pixel one as paired
+// instructions with the same per-half rounding), so their images are
+// bit-identical.  Against the reference's f32 expression order the per-pixel
 // math differs only in rounding (log2-domain exponent, fused multiply-adds),
 // which the 2/255 image tolerance covers.
 #include <algorithm>
