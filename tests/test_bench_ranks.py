@@ -7,8 +7,6 @@ import sys
 from pathlib import Path
 
 import numpy as np
-import pytest
-import torch
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
