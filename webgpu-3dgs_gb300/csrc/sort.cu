@@ -28,6 +28,7 @@
 // (tile id, depth bits, emit position), since every pass is a stable
 // counting sort on one digit.
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 
 #include "gs3d_internal.cuh"
@@ -660,7 +661,11 @@ __global__ void __launch_bounds__(kWideThreads, 1)
 }
 
 cudaError_t onesweep_wide_setup() {
-  static bool done = false;  // per process: the library drives one device
+  // once per process (the library drives one device); contexts on other
+  // host threads may launch concurrently
+  static std::mutex mu;
+  static bool done = false;
+  std::lock_guard<std::mutex> lock(mu);
   if (!done) {
     cudaError_t e = cudaFuncSetAttribute(onesweep_wide_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -673,7 +678,11 @@ cudaError_t onesweep_wide_setup() {
 
 template <typename K, int NBITS>
 cudaError_t onesweep_setup(int* per_sm) {
-  static int v = 0;  // per process: the library drives one device
+  // once per process and instantiation (the library drives one device);
+  // contexts on other host threads may launch concurrently
+  static std::mutex mu;
+  static int v = 0;
+  std::lock_guard<std::mutex> lock(mu);
   if (v == 0) {
     cudaError_t e = cudaFuncSetAttribute(onesweep_kernel<K, NBITS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
