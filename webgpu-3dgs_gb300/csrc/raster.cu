@@ -198,10 +198,11 @@ __device__ __forceinline__ void stage_batch(const gs3d_projected_splat* __restri
 // form's minimum over a box not holding the mean lies on an edge, at the
 // clamped stationary point of that edge), compared with vis; plus the radius
 // circle.  Conservative by the margins folded into vis and the circle.
-__device__ __forceinline__ bool rect_may_hit(const SplatStage& s, float xlo, float xhi, float ylo,
-                                             float yhi) {
+__device__ __forceinline__ bool rect_may_hit(const SplatStage& s, float2 xr, float2 yr) {
   const float4 a = s.a, b = s.b;
-  const float x0 = xlo - a.x, x1 = xhi - a.x, y0 = ylo - a.y, y1 = yhi - a.y;
+  // the box corners relative to the mean (x - m computed as x + (-m))
+  const float2 xd = __fadd2_rn(xr, bcast(-a.x)), yd = __fadd2_rn(yr, bcast(-a.y));
+  const float x0 = xd.x, x1 = xd.y, y0 = yd.x, y1 = yd.y;
   const float ex = fminf(fmaxf(0.0f, x0), x1), ey = fminf(fmaxf(0.0f, y0), y1);
   if (ex * ex + ey * ey > a.z * 1.0001f + 1e-3f) return false;
   const float vis = b.w;
@@ -215,7 +216,7 @@ __device__ __forceinline__ bool rect_may_hit(const SplatStage& s, float xlo, flo
   const float sy = __fdividef(-qb, 2.0f * qc), sx = __fdividef(-qb, 2.0f * qa);
   // Q = qa x^2 + qb x y + qc y^2 at the two vertical edges (x0, x1 at their
   // clamped stationary y) and the two horizontal ones, as pairs
-  const float2 vx = make_float2(x0, x1), hy = make_float2(y0, y1);
+  const float2 vx = xd, hy = yd;
   const float2 svy = __fmul2_rn(bcast(sy), vx), shx = __fmul2_rn(bcast(sx), hy);
   const float2 vy = make_float2(fminf(fmaxf(svy.x, y0), y1), fminf(fmaxf(svy.y, y0), y1));
   const float2 hx = make_float2(fminf(fmaxf(shx.x, x0), x1), fminf(fmaxf(shx.y, x0), x1));
@@ -359,7 +360,7 @@ __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, Splat
     if (__any_sync(0xffffffffu, !done)) {
       for (uint32_t k0 = 0; k0 < cnt; k0 += 32) {
         const uint32_t j = k0 + lane;
-        const bool hit = j < cnt && rect_may_hit(cur[j], xlo, xhi, ylo, yhi);
+        const bool hit = j < cnt && rect_may_hit(cur[j], make_float2(xlo, xhi), make_float2(ylo, yhi));
         uint32_t mask = __ballot_sync(0xffffffffu, hit);
         while (mask) {
           const uint32_t b0 = __ffs(mask) - 1;
@@ -451,7 +452,7 @@ __device__ void raster_tile_culled2(const RasterArgs& a, const TileGeom& g, uint
     if (__any_sync(0xffffffffu, !(done0 && done1))) {
       for (uint32_t k0 = 0; k0 < cnt; k0 += 32) {
         const uint32_t j = k0 + lane;
-        const bool hit = j < cnt && rect_may_hit(cur[j], xlo, xhi, ylo, yhi);
+        const bool hit = j < cnt && rect_may_hit(cur[j], make_float2(xlo, xhi), make_float2(ylo, yhi));
         uint32_t mask = __ballot_sync(0xffffffffu, hit);
         while (mask) {
           const uint32_t b = __ffs(mask) - 1;
