@@ -176,13 +176,18 @@ def cpu_c0_stages(threads):
             "stage_ms": {k: round(v * 1e3, 2) for k, v in t.items()}}
 
 
-def algorithmic_bytes(n, R, tiles, tile_passes, sh_floats, fused):
+def algorithmic_bytes(n, R, tiles, tile_passes, sh_floats, fused, views_per_scene=1):
     """Minimum bytes each stage must move for one view (inputs read once,
-    outputs written once), the numerator of the per-stage roofline."""
+    outputs written once), the numerator of the per-stage roofline.  The
+    batched preprocess reads a scene's splats once per launch for all
+    `views_per_scene` views of it, so a view is charged that share of the read."""
     full_passes = 4 + tile_passes
     return {
-        # fused: + depth key, depth id and the one-word tile rectangle per splat-view
-        "preprocess-splats": n * (64 + 4 * sh_floats) + n * (64 + 4 + (12 if fused else 0)),
+        # splat SoA (64 B) + SH rest read once per scene and launch; per
+        # splat-view the record and count, fused: + depth key, depth id and
+        # the one-word tile rectangle
+        "preprocess-splats": n * (64 + 4 * sh_floats) / views_per_scene
+                             + n * (64 + 4 + (12 if fused else 0)),
         "depth-sort": 4 * n + 4 * 16 * n,
         "prefix-scan": 12 * n if fused else 8 * n,
         # fused: depth id, depth key, offset and one-word rectangle per splat-view
@@ -214,6 +219,27 @@ def dominant_traffic(stage, tile, refs_per_launch, splats_per_launch, scene_spla
         b, n, r = DRAM_EMIT[tile]
         return int(b * (0.5 * splats_per_launch / n + 0.5 * refs_per_launch / r))
     return None
+
+
+# Pipe use of the raster kernel (ncu --set full, one launch of the headline
+# path's raster at 32x32 tiles; profiles/raster_culled_3M_sh3_1080p.md).
+RASTER_NCU = {"kernel": "raster_kernel_culled2", "issue_active": 0.728, "pipe_fma": 0.466,
+              "pipe_alu": 0.608, "warps_active": 0.496,
+              "source": "profiles/raster_culled_3M_sh3_1080p.md"}
+
+
+def raster_work(view=0, tile=TILE):
+    """(pixel, splat) pairs of the reference raster loop on one full-size view,
+    counted by the oracle: iterated (tile lists walked up to each pixel's
+    termination), exp evaluated, blended."""
+    from oracle import Oracle
+    o = Oracle()
+    data, cams = make_workload(view + 1)
+    r = o.rebin(cams[view], WIDTH, HEIGHT, tile, tile, data.positions, data.scales,
+                data.rotations, data.colors, data.sphericalHarmonics, 3,
+                key_capacity=N_SPLATS * 16)
+    return o.raster_pairs(WIDTH, HEIGHT, tile, tile, r["projected_splats"], r["tile_offsets"],
+                          r["sort_values_a"])
 
 
 def install_cost_model(lib, ctx, tile):
@@ -473,8 +499,8 @@ def run_ours(args, rank, world):
     mean_R = float(np.mean(refs))
     peak, peak_kind = peaks()
 
-    def roof(stages, fused, R, tiles, passes, tile_px):
-        algo = algorithmic_bytes(N_SPLATS, R, tiles, passes, 45, fused)
+    def roof(stages, fused, R, tiles, passes, tile_px, views_per_scene=1):
+        algo = algorithmic_bytes(N_SPLATS, R, tiles, passes, 45, fused, views_per_scene)
         out = {}
         for name, (ms, n) in stages.items():
             gbs = algo[name] / (ms * 1e-3) / 1e9
@@ -482,7 +508,7 @@ def run_ours(args, rank, world):
                          "frac_hbm": round(gbs / peak, 3)}
         return out
 
-    batched_roof = roof(batched_stages, True, tuned_R, tiles_t, tuned_passes, tuned.tile_w)
+    batched_roof = roof(batched_stages, True, tuned_R, tiles_t, tuned_passes, tuned.tile_w, B)
     hbm = [s for s in batched_roof if s != "rasterize-tiles"]
     dom = max(hbm, key=lambda s: batched_roof[s]["ms"])
     learned_on = batched_schedule == _lib.SCHEDULE_LEARNED
@@ -629,6 +655,18 @@ def main():
                                 f"threads_{Oracle().max_threads()}":
                                     cpu_c0_stages(Oracle().max_threads()),
                                 "gpu_single_view_fused_views_per_s": res["c0_gpu_views_per_s"]}}
+    raster_roof = None
+    if rank == 0:
+        # the raster is issue-bound: its pipe use (ncu) and the reference
+        # loop's work on view 0 against the headline path's raster time
+        rms = res["per_stage"]["rasterize-tiles"]["ms"]
+        raster_roof = dict(RASTER_NCU, bound="issue (FMA/ALU/SFU pipes)", ms_per_view=rms)
+        if not args.no_cpu_baseline:
+            pairs = raster_work(0, TILE)
+            raster_roof.update(
+                pairs_per_view=pairs, pairs_view="orbit pose 0, 16x16 tiles, oracle count",
+                blended_pairs_per_s=round(pairs["blended"] / (rms * 1e-3), 1),
+                evaluated_pairs_per_s=round(pairs["evaluated"] / (rms * 1e-3), 1))
     if rank == 0:
         dom = res["per_stage"][res["dominant"]]
         out = {
@@ -660,6 +698,7 @@ def main():
                          "traffic_per": "launch (one pass over one batch), ncu DRAM "
                                         "bytes of a 2-view capture scaled by units",
                          "launch_units": res["launch_units"]},
+            "roofline_raster": raster_roof,
             "stages": res["per_stage"],
             "stages_single_view_fused": res["fused_stages"],
             "stages_plain_stagewise": res["stagewise_stages"],

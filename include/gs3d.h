@@ -408,9 +408,27 @@ int gs3d_read_tile_counts(struct gs3d_ctx* ctx, uint32_t* counts, size_t n);
  *     address (set-up), so make it before any stream capture;
  *   - every call on a device shares the one scratch array: calls whose
  *     kernels overlap on the GPU (different streams, no ordering between
- *     them) race and give wrong offsets; order them on one stream. */
+ *     them) race and give wrong offsets; order them on one stream;
+ *   - the scratch address is looked up once per device and kept: do not
+ *     reset the device (cudaDeviceReset) while the library is loaded;
+ *   - GS3D_OK means the scan was enqueued, not that it succeeded: the device
+ *     errors it can meet (a total of 2^32 or more, a look-back wait that gave
+ *     up) are latched in the scratch array and reported by
+ *     gs3d_prefix_scan_noalloc_status. */
 int gs3d_prefix_scan_noalloc(const uint32_t* counts, uint32_t* offsets, uint32_t n,
                              void* stream);
+/* No counterpart in the reference.  Device errors of the last
+ * gs3d_prefix_scan_noalloc call on the current device, read behind the work
+ * already enqueued on `stream` (the call waits for that stream):
+ *   GS3D_OK            the offsets are complete and exact;
+ *   GS3D_ERR_CAPACITY  the counts sum to 2^32 or more: offsets[n] holds
+ *                      0xffffffff and the offsets past the overflow are not
+ *                      valid;
+ *   GS3D_ERR_TIMEOUT   a bounded look-back wait gave up: the offsets are
+ *                      incomplete.
+ * Like the scan itself it allocates nothing.  With calls on several streams
+ * of one device it reports whichever call wrote the scratch array last. */
+int gs3d_prefix_scan_noalloc_status(void* stream);
 
 #ifdef __cplusplus
 }

@@ -530,6 +530,51 @@ void orc_rasterize(uint32_t width, uint32_t height, uint32_t tile_w,
   }
 }
 
+// Work counts of rasterize_tiles.wgsl:44-110 over a frame (the same loop as
+// orc_rasterize, counting instead of shading): out[0] = (pixel, splat) pairs
+// the reference iterates (every splat of the pixel's tile up to the pixel's
+// termination), out[1] = pairs inside the radius with power <= 0 (an exp is
+// evaluated, :85-92), out[2] = pairs blended (:95-96).
+void orc_raster_pairs(uint32_t width, uint32_t height, uint32_t tile_w, uint32_t tile_h,
+                      uint32_t tiles_x, uint32_t tiles_y, const void* projected,
+                      const uint32_t* tile_offsets, const uint32_t* values, uint64_t out[3],
+                      int threads) {
+  const Projected* ps = static_cast<const Projected*>(projected);
+  const int nt = resolve_threads(threads);
+  const long long ntiles = (long long)tiles_x * tiles_y;
+  uint64_t it = 0, ev = 0, bl = 0;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nt) reduction(+ : it, ev, bl)
+  for (long long t = 0; t < ntiles; ++t) {
+    const uint32_t tx = (uint32_t)(t % tiles_x), ty = (uint32_t)(t / tiles_x);
+    const uint32_t start = tile_offsets[t], end = tile_offsets[t + 1];
+    for (uint32_t ly = 0; ly < tile_h; ++ly)
+      for (uint32_t lx = 0; lx < tile_w; ++lx) {
+        const uint32_t px = tx * tile_w + lx, py = ty * tile_h + ly;
+        if (px >= width || py >= height) continue;
+        const float pfx = (float)px + 0.5f, pfy = (float)py + 0.5f;
+        float T = 1.0f;
+        for (uint32_t j = start; j < end; ++j) {
+          ++it;
+          const Projected& s = ps[values[j]];
+          const float dx = pfx - s.mean_px[0], dy = pfy - s.mean_px[1];
+          if (dx * dx + dy * dy > s.radius_px * s.radius_px) continue;
+          const float power = -0.5f * (s.conic[0] * dx * dx + 2.0f * s.conic[1] * dx * dy +
+                                       s.conic[2] * dy * dy);
+          if (power > 0.0f) continue;
+          ++ev;
+          const float alpha = std::min(0.99f, s.opacity * std::exp(power));
+          if (alpha < 1.0f / 255.0f) continue;
+          ++bl;
+          T *= 1.0f - alpha;
+          if (T < 1.0e-4f) break;
+        }
+      }
+  }
+  out[0] = it;
+  out[1] = ev;
+  out[2] = bl;
+}
+
 uint32_t orc_rebin(uint32_t n, const float cam[72], uint32_t width,
                    uint32_t height, uint32_t tile_w, uint32_t tile_h,
                    const float* positions, const float* scales,

@@ -65,6 +65,13 @@ void orc_rasterize(uint32_t width, uint32_t height, uint32_t tile_w,
                    const uint32_t* values, float* image, uint32_t* tile_costs,
                    int threads);
 
+/* Work counts of the same loop: out = {pairs iterated, pairs whose exp is
+ * evaluated (inside the radius, power <= 0), pairs blended}. */
+void orc_raster_pairs(uint32_t width, uint32_t height, uint32_t tile_w, uint32_t tile_h,
+                      uint32_t tiles_x, uint32_t tiles_y, const void* projected,
+                      const uint32_t* tile_offsets, const uint32_t* values, uint64_t out[3],
+                      int threads);
+
 /* Whole rebin in one call with caller-provided buffers; returns R, or
  * 0xFFFFFFFF when R exceeds key_capacity (nothing past the scan is run). */
 uint32_t orc_rebin(uint32_t n, const float cam[72], uint32_t width,

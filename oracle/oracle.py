@@ -48,6 +48,7 @@ class Oracle:
         lib.orc_rebin.argtypes = ([u32, _P, u32, u32, u32, u32] + [_P] * 5 +
                                   [u32, _P, _P, _P, u32, _P, _P, _P, _P, _P, _P, _P, i32])
         lib.orc_rebin.restype = u32
+        lib.orc_raster_pairs.argtypes = [u32, u32, u32, u32, u32, u32, _P, _P, _P, _P, i32]
         lib.orc_max_threads.restype = i32
         self.lib = lib
 
@@ -119,6 +120,17 @@ class Oracle:
                                _ptr(np.ascontiguousarray(proj)), _ptr(_c(tile_offsets, np.uint32)),
                                _ptr(_c(vals, np.uint32)), _ptr(img), _ptr(costs), threads)
         return img, costs
+
+    def raster_pairs(self, width, height, tile_w, tile_h, proj, tile_offsets, vals, threads=0):
+        """(pixel, splat) pairs of the reference raster loop: iterated, exp
+        evaluated, blended."""
+        tx, ty = -(-width // tile_w), -(-height // tile_h)
+        out = np.zeros(3, np.uint64)
+        self.lib.orc_raster_pairs(width, height, tile_w, tile_h, tx, ty,
+                                  _ptr(np.ascontiguousarray(proj)),
+                                  _ptr(_c(tile_offsets, np.uint32)), _ptr(_c(vals, np.uint32)),
+                                  _ptr(out), threads)
+        return {"iterated": int(out[0]), "evaluated": int(out[1]), "blended": int(out[2])}
 
     def rebin(self, cam, width, height, tile_w, tile_h, pos, scale, rot, color, sh=None,
               sh_degree=0, threads=0, key_capacity=None):

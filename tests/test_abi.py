@@ -53,6 +53,13 @@ def test_null_arguments_are_rejected(built_lib):
 
 
 @pytest.mark.skipif(has_gpu(), reason="checks the no-device path")
+def test_noalloc_status_without_device_is_a_status_code(built_lib):
+    from gs3d import _lib
+    lib = _lib.load()
+    assert lib.gs3d_prefix_scan_noalloc_status(None) == _lib.ERR_NO_DEVICE
+
+
+@pytest.mark.skipif(has_gpu(), reason="checks the no-device path")
 def test_create_without_device_reports_no_device(built_lib):
     from gs3d import _lib
     lib = _lib.load()

@@ -185,6 +185,32 @@ def test_raster_early_termination_and_cost(oracle):
     assert costs[0] == 3                 # but other pixels of the tile iterate all three
 
 
+def _pairs_one(oracle, splats):
+    proj = np.zeros(len(splats), PROJ_DTYPE)
+    for i, (mx, my, r, conic, op, col) in enumerate(splats):
+        proj[i]["mean_px"] = (mx, my)
+        proj[i]["radius_px"] = r
+        proj[i]["conic"] = conic
+        proj[i]["opacity"] = op
+        proj[i]["color"] = col
+        proj[i]["valid"] = 1
+    toff = np.array([0, len(splats)], np.uint32)
+    return oracle.raster_pairs(16, 16, 16, 16, proj, toff, np.arange(len(splats), dtype=np.uint32))
+
+
+def test_raster_pair_counts(oracle):
+    # one splat of radius 0.5: every pixel iterates it, only the centre pixel
+    # is inside the radius (|d|^2 = 0; all others >= 1 > 0.25) and blends it
+    assert _pairs_one(oracle, [(8.5, 8.5, 0.5, (1e-6, 0.0, 1e-6), 0.9, (1, 1, 1))]) == \
+        {"iterated": 256, "evaluated": 1, "blended": 1}
+    # three near-opaque unit-conic splats at the centre: every pixel is inside
+    # the radius with power <= 0; alpha >= 1/255 where |d|^2 <= 10 (37 pixels);
+    # the centre pixel terminates at the second splat, the others walk all 3
+    spl = [(8.5, 8.5, 100.0, (1.0, 0.0, 1.0), 0.99, (1.0, 0.0, 0.0))] * 3
+    assert _pairs_one(oracle, spl) == \
+        {"iterated": 255 * 3 + 2, "evaluated": 255 * 3 + 2, "blended": 36 * 3 + 2}
+
+
 def test_activations_match_loader(oracle):
     from gs3d.scenes import activate
     rng = np.random.default_rng(0)

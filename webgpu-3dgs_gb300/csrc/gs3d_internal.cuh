@@ -180,6 +180,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 
 __device__ __forceinline__ void latch_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }
 
+// Per-device launch set-up (shared-memory attributes, occupancy) is cached
+// in arrays of this many devices.
+constexpr int kMaxDevices = 64;
+// The calling thread's current device, checked against kMaxDevices.
+inline cudaError_t current_device(int* dev) {
+  const cudaError_t e = cudaGetDevice(dev);
+  if (e != cudaSuccess) return e;
+  return (*dev < 0 || *dev >= kMaxDevices) ? cudaErrorInvalidDevice : cudaSuccess;
+}
+
 // Shared-memory histogram add with a warp-uniform fast path: coherent digits
 // (the high byte of neighbouring tile ids, a depth exponent byte) would
 // otherwise serialise the lanes of a warp on one address.  Every lane of the

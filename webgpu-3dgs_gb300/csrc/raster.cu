@@ -561,10 +561,17 @@ cudaError_t launch_raster(const RasterArgs& args, int sm_count, cudaStream_t s) 
   const size_t smem = 2 * (size_t)D * sizeof(SplatStage);
   auto kern = mode == 2 ? raster_kernel_culled2 : mode == 1 ? raster_kernel_culled
                                                              : raster_kernel_plain;
-  // launch configuration per (variant, tile area, batch), computed once per process
+  // launch configuration per (device, variant, tile area, batch), computed
+  // once per process (the shared-memory attribute is a per-device setting)
   static std::mutex mu;
   static std::map<uint64_t, int> cache;
-  const uint64_t key = ((uint64_t)mode << 40) | ((uint64_t)threads << 20) | D;
+  int dev = 0;
+  {
+    const cudaError_t e = current_device(&dev);
+    if (e != cudaSuccess) return e;
+  }
+  const uint64_t key = ((uint64_t)dev << 48) | ((uint64_t)mode << 40) |
+                       ((uint64_t)threads << 20) | D;
   int per_sm = 0;
   {
     std::lock_guard<std::mutex> lock(mu);

@@ -18,7 +18,6 @@ namespace {
 constexpr uint32_t kNoAllocMaxCounts = 1u << 26;  // 67,108,864 counts per call
 constexpr uint32_t kScanTileCounts = 2048;        // counts per look-back tile (scan.cu)
 constexpr uint32_t kNoAllocTiles = kNoAllocMaxCounts / kScanTileCounts + 1;
-constexpr int kMaxDevices = 64;
 
 struct NoAllocScratch {
   unsigned long long status[kNoAllocTiles];  // epoch-tagged look-back words (256 KB)
@@ -32,8 +31,8 @@ struct NoAllocScratch {
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
 std::mutex g_mutex;
-NoAllocScratch* g_scratch_ptr[kMaxDevices] = {};  // device address, per device
-uint32_t g_epoch[kMaxDevices] = {};               // look-back epoch, per device
+NoAllocScratch* g_scratch_ptr[gs3d::kMaxDevices] = {};  // device address, per device
+uint32_t g_epoch[gs3d::kMaxDevices] = {};               // look-back epoch, per device
 thread_local char g_error[256] = "no error";
 
 int fail(int code, const char* msg) {
@@ -61,7 +60,7 @@ extern "C" int gs3d_prefix_scan_noalloc(const uint32_t* counts, uint32_t* offset
   }
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+  if (e != cudaSuccess || dev < 0 || dev >= gs3d::kMaxDevices)
     return fail(GS3D_ERR_NO_DEVICE, "gs3d_prefix_scan_noalloc: no current CUDA device");
   NoAllocScratch* scratch = nullptr;
   uint32_t epoch = 0;
@@ -98,5 +97,41 @@ extern "C" int gs3d_prefix_scan_noalloc(const uint32_t* counts, uint32_t* offset
     cudaGetLastError();
     return fail(GS3D_ERR_CUDA, msg);
   }
+  return GS3D_OK;
+}
+
+// The device errors of the last gs3d_prefix_scan_noalloc call on the current
+// device: the error word is copied out behind the work already on `stream`
+// (into pageable host memory, so the copy has landed when it returns).
+extern "C" int gs3d_prefix_scan_noalloc_status(void* stream) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= gs3d::kMaxDevices)
+    return fail(GS3D_ERR_NO_DEVICE, "gs3d_prefix_scan_noalloc_status: no current CUDA device");
+  NoAllocScratch* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    scratch = g_scratch_ptr[dev];
+  }
+  if (scratch == nullptr) return GS3D_OK;  // no scan has run on this device
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  uint32_t word = 0;
+  e = cudaMemcpyAsync(&word, &scratch->error, sizeof(word), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    char msg[200];
+    snprintf(msg, sizeof(msg), "gs3d_prefix_scan_noalloc_status: reading the error word failed: %s",
+             cudaGetErrorString(e));
+    cudaGetLastError();
+    return fail(GS3D_ERR_CUDA, msg);
+  }
+  if (word & gs3d::DEVERR_CAPACITY)
+    return fail(GS3D_ERR_CAPACITY,
+                "gs3d_prefix_scan_noalloc: the counts sum to 2^32 or more; offsets[n] was "
+                "written as 0xffffffff and the offsets past the overflow are not valid");
+  if (word & gs3d::DEVERR_TIMEOUT)
+    return fail(GS3D_ERR_TIMEOUT,
+                "gs3d_prefix_scan_noalloc: a bounded look-back wait gave up; the offsets are "
+                "incomplete");
   return GS3D_OK;
 }

@@ -22,7 +22,7 @@
 // in the B buffers and the host swaps the buffer names.
 //
 // The same pass kernel, instantiated for 32-bit keys, sorts the per-splat
-// depth keys of the fused rebin (rebin.cu).
+// depth keys of the fused rebin (fused_rebin in ctx.cu).
 //
 // The order produced is identical to the reference's: lexicographic
 // (tile id, depth bits, emit position), since every pass is a stable
@@ -661,40 +661,44 @@ __global__ void __launch_bounds__(kWideThreads, 1)
 }
 
 cudaError_t onesweep_wide_setup() {
-  // once per process (the library drives one device); contexts on other
-  // host threads may launch concurrently
+  // once per device (the attribute is a per-device setting); contexts on
+  // other host threads may launch concurrently
   static std::mutex mu;
-  static bool done = false;
+  static bool done[kMaxDevices] = {};
+  int dev = 0;
+  cudaError_t e = current_device(&dev);
+  if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lock(mu);
-  if (!done) {
-    cudaError_t e = cudaFuncSetAttribute(onesweep_wide_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)wide_pass_smem<uint2>());
+  if (!done[dev]) {
+    e = cudaFuncSetAttribute(onesweep_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)wide_pass_smem<uint2>());
     if (e != cudaSuccess) return e;
-    done = true;
+    done[dev] = true;
   }
   return cudaSuccess;
 }
 
 template <typename K, int NBITS>
 cudaError_t onesweep_setup(int* per_sm) {
-  // once per process and instantiation (the library drives one device);
-  // contexts on other host threads may launch concurrently
+  // once per device and instantiation (the attribute is a per-device
+  // setting); contexts on other host threads may launch concurrently
   static std::mutex mu;
-  static int v = 0;
+  static int v[kMaxDevices] = {};
+  int dev = 0;
+  cudaError_t e = current_device(&dev);
+  if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lock(mu);
-  if (v == 0) {
-    cudaError_t e = cudaFuncSetAttribute(onesweep_kernel<K, NBITS>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)pass_smem<K>());
+  if (v[dev] == 0) {
+    e = cudaFuncSetAttribute(onesweep_kernel<K, NBITS>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pass_smem<K>());
     if (e != cudaSuccess) return e;
     int n = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, onesweep_kernel<K, NBITS>,
                                                       kPassThreads, pass_smem<K>());
     if (e != cudaSuccess) return e;
-    v = n > 0 ? n : 1;
+    v[dev] = n > 0 ? n : 1;
   }
-  *per_sm = v;
+  *per_sm = v[dev];
   return cudaSuccess;
 }
 

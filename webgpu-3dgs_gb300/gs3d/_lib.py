@@ -136,6 +136,7 @@ SIGNATURES = {
     "gs3d_ref_count": ([_P, C.POINTER(_U32)], _I),
     "gs3d_read_tile_counts": ([_P, _P, _SZ], _I),
     "gs3d_prefix_scan_noalloc": ([_P, _P, _U32, _P], _I),
+    "gs3d_prefix_scan_noalloc_status": ([_P], _I),
     "gs3d_ply_inspect": ([_P, _SZ, C.POINTER(PlyInfo_t)], _I),
     "gs3d_read_buffer_range": ([_P, _I, _SZ, _P, _SZ], _I),
     "gs3d_composite": ([_P, _U32, _U32, _U32, _P, _P, _SZ, _I], _I),
