@@ -4,7 +4,11 @@ Every translation unit is compiled by nvcc for sm_103a only, in parallel, and
 linked into one shared library with a static CUDA runtime.  preprocess.cu is
 compiled with -fmad=false so its f32 arithmetic is one IEEE-rounded
 operation per written operator, the property its bit-exact parity with the
-CPU oracle relies on; the other stages use the default contraction.
+CPU oracle relies on; the other stages use the default contraction.  Where
+the raster must not contract (its reference-order form of d^T conic d) it
+uses the scalar __fmul_rn / __fadd_rn intrinsics, which are never fused: a
+paired FP32 multiply feeding a paired add is fused into a paired FMA on
+sm_103a, with or without -fmad=false.
 """
 from __future__ import annotations
 
@@ -40,7 +44,9 @@ def sources() -> list[Path]:
 
 def _compile(src: Path, verbose: bool) -> Path:
     obj = BUILD_DIR / (src.stem + ".o")
-    deps = [src] + sorted(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "gs3d.h"]
+    # the flags live here, so a change of this file recompiles everything
+    deps = [src] + sorted(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "gs3d.h",
+                                                  Path(__file__).resolve()]
     if obj.exists() and obj.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
         return obj
     cmd = [nvcc(), *ARCH, *COMMON, *PER_FILE.get(src.name, []), "-c", str(src), "-o", str(obj)]

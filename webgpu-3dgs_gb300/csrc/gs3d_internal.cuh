@@ -162,20 +162,34 @@ __device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gmem_src, u
       "l"(gmem_src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
-// Bounded parity wait; returns false if the limit ran out.
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Device waits on an mbarrier give up after this much wall time (and the
+// caller latches DEVERR_TIMEOUT).
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
+// Bounded parity wait; returns false if the limit ran out.  Each try_wait
+// may suspend the thread until the phase completes (up to the hint, 1 ms),
+// so waiting threads issue almost nothing; the wait is bounded by
+// kWaitLimitNs of wall time.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+  uint64_t t0 = 0;
+  for (;;) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(1000000u)
         : "memory");
     if (ok) return true;
-    if (i > 64) __nanosleep(64);
+    const uint64_t t = global_ns();
+    if (t0 == 0) t0 = t;
+    else if (t - t0 > kWaitLimitNs) return false;
   }
-  return false;
 }
 
 __device__ __forceinline__ void latch_error(uint32_t* err, uint32_t bit) { atomicOr(err, bit); }

@@ -15,10 +15,11 @@
 //    one is blended;
 //  * the CTA leaves as soon as a block-wide vote finds every pixel
 //    terminated (the reference keeps looping over the remaining batches);
-//  * each staged splat is converted once per tile into pre-scaled conic
-//    coefficients, so a (pixel, splat) pair costs one ex2 and a branch-free
-//    handful of FMAs (a skipped splat blends with alpha = 0, which leaves the
-//    pixel bit-unchanged);
+//  * each staged splat is converted once per tile into its raster form (r^2,
+//    the quadratic form's coefficients, the visibility bound), so a (pixel,
+//    splat) pair costs one ex2 and a branch-free handful of FP32 operations
+//    (a skipped splat blends with alpha = 0, which leaves the pixel
+//    bit-unchanged);
 //  * (culled variant) each warp owns a compact pixel block (8x4 for tiles
 //    whose sides divide by 8 and 4) and tests every staged splat once against
 //    it; a splat is skipped for the whole warp only when no pixel centre of
@@ -38,9 +39,12 @@
 //
 // The variants share the per-pixel arithmetic (the two-pixel one as paired
 // instructions with the same per-half rounding), so their images are
-// bit-identical.  Against the reference's f32 expression order the per-pixel
-// math differs only in rounding (log2-domain exponent, fused multiply-adds),
-// which the 2/255 image tolerance covers.
+// bit-identical.  For splats whose quadratic form can cancel badly the
+// radius test and power = -0.5 d^T conic d follow the reference's f32
+// expression order exactly (no contraction; SplatStage below); the others,
+// the exponent (ex2 in the log2 domain) and the blend (fused multiply-adds)
+// differ from the reference only in rounding, which the 2/255 image
+// tolerance covers.
 #include <algorithm>
 #include <map>
 #include <mutex>
@@ -50,11 +54,29 @@
 namespace gs3d {
 namespace {
 
+// A staged splat in one of two forms of the quadratic form q(d) = b.x dx^2 +
+// b.y dx dy + b.z dy^2 (c.w says which):
+//   fast  (c.w = 0): b = log2(e)/2 (conic.x, 2 conic.y, conic.z), q = Q =
+//         -power log2(e), evaluated with FMAs;
+//   exact (c.w = 1): b = (conic.x, 2 conic.y, conic.z), q = s = d^T conic d
+//         = -2 power, evaluated in the reference's operation order without
+//         contraction (every sum a scalar __fadd_rn: a paired FP32 multiply
+//         feeding a paired add is contracted into a paired FMA).
+// Splats take the exact form when the terms of q can reach 2^12 inside the
+// radius, (|conic.x| + 2 |conic.y| + |conic.z|) r^2 > 2^12: there the terms
+// cancel (elongated splats seen far from their mean), and the rounding order
+// decides the result.  Below that bound the fast form's q differs from the
+// reference's by about 2^-11 at most, so each alpha differs by a relative
+// 1e-3 and a pixel, whose blend weights alpha_i T_i sum to at most 1, by
+// about that much.  b.w = vis, in q's units.
 struct SplatStage {  // first 48 bytes of a ProjectedSplat, prepared in place (prepare())
   float4 a;  // mean_px.x, mean_px.y, radius_px^2, opacity
-  float4 b;  // qa, qb, qc, vis: Q(d) = qa dx^2 + qb dx dy + qc dy^2 = log2(e)/2 * d^T conic d
-  float4 c;  // color.xyz, unused
+  float4 b;  // q coefficients (see above), vis
+  float4 c;  // color.xyz, form
 };
+
+constexpr float kHalfLog2e = 0.72134752044448170f;
+constexpr float kExactFormBound = 4096.0f;
 
 struct Pixel {
   float cr, cg, cb, T;
@@ -69,39 +91,56 @@ __device__ __forceinline__ float ex2_approx(float x) {
 
 // Converts the staged ProjectedSplat prefix (mean, depth, radius | conic,
 // opacity | color, valid) into the raster form.  vis = the largest Q at which
-// alpha can still reach 1/255, with a 1% margin (-1: never visible; +inf:
-// conic too ill-conditioned for the alpha bound, use the circle only).
+// alpha can still reach 1/255, with a 1% margin, in the units of the splat's
+// form (-1: never visible; +inf: conic too ill-conditioned for the alpha
+// bound, or a non-finite opacity or conic: use the circle only).
 __device__ __forceinline__ void prepare(SplatStage& s) {
   const float4 a = s.a, b = s.b;
-  const float k = 0.72134752044448170f;  // log2(e) / 2
   const float A = b.x, B = b.y, C = b.z, op = b.w;
   float vis;
   const float lim = op * 255.0f;
-  if (!(lim > 1.0f)) {
+  if (lim < 0.999f) {
     vis = -1.0f;  // alpha = opacity * exp(power) <= opacity < 1/255 everywhere
-  } else if (A * C - B * B >= 1e-3f * (A + C) * (A + C) && A > 0.0f && C > 0.0f) {
+  } else if (lim > 1.0f && A * C - B * B >= 1e-3f * (A + C) * (A + C) && A > 0.0f && C > 0.0f) {
     vis = __log2f(lim) * 1.01f + 1e-3f;
   } else {
     vis = __int_as_float(0x7f800000);
   }
-  s.a = make_float4(a.x, a.y, a.w * a.w, op);
-  s.b = make_float4(k * A, 2.0f * k * B, k * C, vis);
+  const float r2 = a.w * a.w;
+  const float terms = (fabsf(A) + 2.0f * fabsf(B) + fabsf(C)) * r2;
+  s.a = make_float4(a.x, a.y, r2, op);
+  if (terms <= kExactFormBound) {
+    s.b = make_float4(kHalfLog2e * A, 2.0f * kHalfLog2e * B, kHalfLog2e * C, vis);
+    s.c.w = 0.0f;
+  } else {  // also non-finite terms
+    s.b = make_float4(A, 2.0f * B, C, vis / kHalfLog2e);
+    s.c.w = 1.0f;
+  }
 }
 
-// rasterize_tiles.wgsl:81-98 for one (pixel, splat) pair, branch-free: a
-// skipped splat contributes alpha = 0, which leaves C and T bit-unchanged.
-// Returns true when the pixel terminates at this splat.
-// The splat's alpha at the pixel centre and whether it passes the per-pixel
-// tests (inside the radius, power <= 0, alpha >= 1/255).
+// rasterize_tiles.wgsl:81-98 for one (pixel, splat) pair: the splat's alpha
+// at the pixel centre and whether it passes the per-pixel tests (not outside
+// the radius, power not > 0, alpha not < 1/255: a NaN passes, as in the
+// reference).  A skipped splat blends with alpha = 0 (blend_alpha), which
+// leaves C and T bit-unchanged.
 __device__ __forceinline__ float splat_alpha(float pfx, float pfy, const SplatStage& s,
                                              bool& ok) {
   const float4 a = s.a, b = s.b;
   const float dx = pfx - a.x;
   const float dy = pfy - a.y;
-  const float d2 = fmaf(dx, dx, dy * dy);
-  const float Q = fmaf(b.x * dx, dx, fmaf(b.y * dx, dy, b.z * dy * dy));  // = -power * log2(e)
-  const float alpha = fminf(0.99f, a.w * ex2_approx(-Q));
-  ok = (d2 <= a.z) && (Q >= 0.0f) && (alpha >= 1.0f / 255.0f);
+  float d2, q, ev;
+  if (s.c.w == 0.0f) {
+    d2 = fmaf(dx, dx, dy * dy);
+    q = fmaf(b.x * dx, dx, fmaf(b.y * dx, dy, b.z * dy * dy));  // = -power * log2(e)
+    ev = -q;
+  } else {  // the reference's order: d^2 = dx dx + dy dy, s = (c0 dx) dx + (2 c1 dx) dy + (c2 dy) dy
+    d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+    q = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(b.x, dx), dx), __fmul_rn(__fmul_rn(b.y, dx), dy)),
+                  __fmul_rn(__fmul_rn(b.z, dy), dy));
+    ev = __fmul_rn(q, -kHalfLog2e);  // exp(-s/2) = 2^(-s log2(e)/2)
+  }
+  const float alpha = fminf(0.99f, a.w * ex2_approx(ev));
+  ok = !(d2 > a.z) && !(q < 0.0f) && !(alpha < 1.0f / 255.0f);
   return alpha;
 }
 
@@ -120,9 +159,11 @@ __device__ __forceinline__ bool blend_alpha(Pixel& p, const float4 c, float alph
 template <bool EARLY_OUT>
 __device__ __forceinline__ bool blend_one(float pfx, float pfy, const SplatStage& s, Pixel& p,
                                           bool live) {
-  if (EARLY_OUT) {  // outside the radius: alpha would be 0
+  if (EARLY_OUT) {  // outside the radius (d^2 as splat_alpha forms it): alpha would be 0
     const float dx = pfx - s.a.x, dy = pfy - s.a.y;
-    if (!(fmaf(dx, dx, dy * dy) <= s.a.z)) return false;
+    const float d2 = s.c.w == 0.0f ? fmaf(dx, dx, dy * dy)
+                                   : __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+    if (d2 > s.a.z) return false;
   }
   bool ok;
   const float alpha = splat_alpha(pfx, pfy, s, ok);
@@ -145,15 +186,28 @@ __device__ __forceinline__ float2 splat_alpha2(float pfx, float2 pfy, const Spla
   const float4 a = s.a, b = s.b;
   const float dx = pfx - a.x;
   const float2 dy = __fadd2_rn(pfy, bcast(-a.y));
-  const float2 d2 = __ffma2_rn(bcast(dx), bcast(dx), __fmul2_rn(dy, dy));
-  const float2 q = __ffma2_rn(bcast(b.x * dx), bcast(dx),
-                              __ffma2_rn(bcast(b.y * dx), dy,
-                                         __fmul2_rn(__fmul2_rn(bcast(b.z), dy), dy)));
-  const float2 e = make_float2(ex2_approx(-q.x), ex2_approx(-q.y));
+  float2 d2, q, ev;
+  if (s.c.w == 0.0f) {  // fast form (splat-uniform branch)
+    d2 = __ffma2_rn(bcast(dx), bcast(dx), __fmul2_rn(dy, dy));
+    q = __ffma2_rn(bcast(b.x * dx), bcast(dx),
+                   __ffma2_rn(bcast(b.y * dx), dy, __fmul2_rn(__fmul2_rn(bcast(b.z), dy), dy)));
+    ev = make_float2(-q.x, -q.y);
+  } else {  // exact form in the reference's order, the column's dx terms shared; the
+            // products are paired, every sum a scalar __fadd_rn (never merged into an FMA)
+    const float dxx = __fmul_rn(dx, dx);
+    const float t1 = __fmul_rn(__fmul_rn(b.x, dx), dx);
+    const float2 dyy = __fmul2_rn(dy, dy);
+    const float2 t2 = __fmul2_rn(bcast(__fmul_rn(b.y, dx)), dy);
+    const float2 t3 = __fmul2_rn(__fmul2_rn(bcast(b.z), dy), dy);
+    d2 = make_float2(__fadd_rn(dxx, dyy.x), __fadd_rn(dxx, dyy.y));
+    q = make_float2(__fadd_rn(__fadd_rn(t1, t2.x), t3.x), __fadd_rn(__fadd_rn(t1, t2.y), t3.y));
+    ev = __fmul2_rn(q, bcast(-kHalfLog2e));
+  }
+  const float2 e = make_float2(ex2_approx(ev.x), ex2_approx(ev.y));
   const float2 am = __fmul2_rn(bcast(a.w), e);
   const float2 alpha = make_float2(fminf(0.99f, am.x), fminf(0.99f, am.y));
-  ok0 = (d2.x <= a.z) && (q.x >= 0.0f) && (alpha.x >= 1.0f / 255.0f);
-  ok1 = (d2.y <= a.z) && (q.y >= 0.0f) && (alpha.y >= 1.0f / 255.0f);
+  ok0 = !(d2.x > a.z) && !(q.x < 0.0f) && !(alpha.x < 1.0f / 255.0f);
+  ok1 = !(d2.y > a.z) && !(q.y < 0.0f) && !(alpha.y < 1.0f / 255.0f);
   return alpha;
 }
 
@@ -194,10 +248,15 @@ __device__ __forceinline__ void stage_batch(const gs3d_projected_splat* __restri
 }
 
 // Can the splat reach alpha >= 1/255 inside the rectangle of pixel centres
-// [x0,x1] x [y0,y1]?  Exact minimum of Q over the rectangle (the quadratic
-// form's minimum over a box not holding the mean lies on an edge, at the
-// clamped stationary point of that edge), compared with vis; plus the radius
-// circle.  Conservative by the margins folded into vis and the circle.
+// [x0,x1] x [y0,y1]?  Exact minimum of the splat's q over the rectangle (the
+// quadratic form's minimum over a box not holding the mean lies on an edge,
+// at the clamped stationary point of that edge; scale-invariant, so either
+// form works), compared with vis; plus the radius circle.  Conservative by
+// the margins folded into vis and the circle: vis is finite only for conics
+// of condition number below about 10^3, where the rounding of q in any
+// operation order stays far inside the 1% margin.  NaN means, radii, conics
+// or opacities are never culled (the per-pixel tests decide, as in the
+// reference).
 __device__ __forceinline__ bool rect_may_hit(const SplatStage& s, float2 xr, float2 yr) {
   const float4 a = s.a, b = s.b;
   // the box corners relative to the mean (x - m computed as x + (-m))
@@ -211,10 +270,10 @@ __device__ __forceinline__ bool rect_may_hit(const SplatStage& s, float2 xr, flo
   if (vis == __int_as_float(0x7f800000)) return true;
   const float qa = b.x, qb = b.y, qc = b.z;
   // edge stationary points, by the fast reciprocal division: an error d in
-  // the point raises Q there by qa d^2 (qc d^2) over the edge minimum, far
+  // the point raises q there by qa d^2 (qc d^2) over the edge minimum, far
   // inside the margins folded into vis
   const float sy = __fdividef(-qb, 2.0f * qc), sx = __fdividef(-qb, 2.0f * qa);
-  // Q = qa x^2 + qb x y + qc y^2 at the two vertical edges (x0, x1 at their
+  // q = qa x^2 + qb x y + qc y^2 at the two vertical edges (x0, x1 at their
   // clamped stationary y) and the two horizontal ones, as pairs
   const float2 vx = xd, hy = yd;
   const float2 svy = __fmul2_rn(bcast(sy), vx), shx = __fmul2_rn(bcast(sx), hy);

@@ -185,12 +185,16 @@ __device__ __forceinline__ uint32_t scan8_inclusive(uint32_t x, int lane) {
 // Claiming cannot deadlock: the smallest unfinished partition is always some
 // CTA's current one, and it waits only on smaller, finished partitions.
 //
-// Three block barriers per partition:
+// Four block barriers per partition:
 //   A  every warp has ranked its items (per-warp digit counts complete, the
 //      input buffer fully read into registers, the fetch landed everywhere);
 //   B  per-digit warp offsets and digit-warp prefix sums are in shared memory;
+//   B' every (warp, digit) entry holds the digit's start in the partition plus
+//      the warp's offset within the digit;
 //   C  the partition is reordered by digit and each digit's global
 //      destination is resolved.
+// Threads waiting for a fetch sleep in mbarrier.try_wait (suspend hint)
+// rather than spinning, so they take no issue slots from the other CTA.
 template <typename K, int NBITS>
 __global__ void __launch_bounds__(kPassThreads, 1024 / kPassThreads)
     onesweep_kernel(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
@@ -323,23 +327,30 @@ __global__ void __launch_bounds__(kPassThreads, 1024 / kPassThreads)
     }
     __syncthreads();  // B
 
-    // exclusive prefix of the eight digit warps' totals, lane w holds warp w's
-    const uint32_t wv = lane < 8 ? s_wsum[lane] : 0u;
-    const uint32_t wex = scan8_inclusive(wv, lane) - wv;
+    // each digit's start in the partition (exclusive prefix of the eight digit
+    // warps' totals + the start within its warp), folded into every warp's
+    // per-digit offset: a partition position is then one table entry plus
+    // the item's rank (positions < 2^16)
+    uint32_t dstart = 0;
+    if (digit_thread) {
+      const uint32_t wv = lane < 8 ? s_wsum[lane] : 0u;
+      const uint32_t wex = scan8_inclusive(wv, lane) - wv;
+      dstart = s_dloc[tid] + __shfl_sync(0xffffffffu, wex, warp);
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w)
+        s_whist[w * kRadixBins + tid] = (uint16_t)(s_whist[w * kRadixBins + tid] + dstart);
+    }
+    __syncthreads();  // B'
 
     // ---- reorder the partition in place ----
 #pragma unroll
     for (int i = 0; i < kItems; ++i) {
-      const uint32_t d = dr[i] & 0xffu;
-      const uint32_t pos =
-          s_dloc[d] + __shfl_sync(0xffffffffu, wex, d >> 5) + wh[d] + (dr[i] >> 8);
+      const uint32_t pos = wh[dr[i] & 0xffu] + (dr[i] >> 8);
       s_keys[pos] = key[i];
       s_vals[pos] = val[i];
     }
 
     // ---- decoupled look-back, one thread per digit ----
-    const uint32_t dstart = digit_thread ? s_dloc[tid] + __shfl_sync(0xffffffffu, wex, warp & 7)
-                                         : 0u;
     uint32_t excl = 0;
     bool ok = true;
     if (digit_thread && part > 0) {
