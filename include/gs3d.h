@@ -97,6 +97,10 @@ typedef struct gs3d_config {
  * same layout only rewrite the view table and replay the graph.  Stage
  * timing events are not recorded in graph mode. */
 #define GS3D_FLAG_CUDA_GRAPH      4u
+/* Shades every tile of the two-pixel raster as half-strip work items (the
+ * split the key-count and learned schedules give their heaviest tiles), for
+ * tests and measurements.  The image is unchanged. */
+#define GS3D_FLAG_SPLIT_ALL_TILES 8u
 
 /* Stage indices of gs3d_read_stage_times (the reference's profiler labels,
  * GaussianSplatRenderer.ts:1144-1260, plus the fused path's depth sort). */
@@ -132,11 +136,30 @@ typedef struct gs3d_view_info {
     uint32_t scene;
 } gs3d_view_info;
 
-/* Raster work order (the persistent raster CTAs pull tiles from a queue). */
+/* Raster work order (the persistent raster CTAs pull tiles from a queue).
+ * The key-count and learned orders also split: tiles whose expected cost
+ * per strip exceeds half of one raster CTA's fair share of the frame (the
+ * head of the order) are shaded as two half-strip work items per strip.
+ * The learned order falls back to the key count on its own while the
+ * measured prediction error exceeds its bound (gs3d_set_schedule_gate). */
 #define GS3D_SCHEDULE_ROW_MAJOR 0u  /* the reference's dispatch order          */
 #define GS3D_SCHEDULE_KEY_COUNT 1u  /* decreasing key count (longest first)    */
 #define GS3D_SCHEDULE_LEARNED   2u  /* decreasing cost predicted by the cost
                                        MLP (gs3d_set_cost_model)               */
+
+/* State of the raster schedule after the last rebin (extension). */
+typedef struct gs3d_schedule_status {
+    uint32_t schedule;     /* requested GS3D_SCHEDULE_*                             */
+    uint32_t active;       /* order the last raster ran in: GS3D_SCHEDULE_KEY_COUNT
+                              when the learned schedule's gate fell back           */
+    float mae_log;         /* running mean |predicted - measured log(1 + cost)| over
+                              all tiles (each frame weighted 1/4, the first as is)  */
+    float last_mae_log;    /* the last learned frame's                              */
+    float bound;           /* the gate's bound on mae_log                           */
+    uint32_t frames;       /* learned frames measured since gs3d_set_cost_model     */
+    uint32_t fallbacks;    /* of those, frames rendered in key-count order          */
+    uint32_t split_tiles;  /* tiles of the last raster shaded as half strips        */
+} gs3d_schedule_status;
 
 /* Cost MLP (extension): 16 tile features -> 64 -> 64 -> 1, ReLU, predicting
  * log(1 + raster cost), the cost being the splats a tile's CTA iterates
@@ -285,6 +308,16 @@ int gs3d_autotune(struct gs3d_ctx* ctx, const gs3d_view* views, uint32_t n_views
  * pointers). */
 int gs3d_set_cost_model(struct gs3d_ctx* ctx, const float* params,
                         const float* feature_mean, const float* feature_std);
+
+/* The learned schedule's fallback gate (extension).  After every learned
+ * raster the library compares the model's predictions with the costs the
+ * raster recorded (tile_costs) on the device; while the running error
+ * exceeds `bound` (mean |log error| over tiles, default 0.5) the next frames
+ * are ordered by key count, and the learned order returns once the error is
+ * back within the bound.  Installing a model resets the running error. */
+int gs3d_set_schedule_gate(struct gs3d_ctx* ctx, float bound);
+/* Schedule state after the last rebin (blocking: waits for the stream). */
+int gs3d_get_schedule_status(struct gs3d_ctx* ctx, gs3d_schedule_status* out);
 
 /* Raw features (n_tiles x 16 f32) of every tile of the last rebin and, in
  * targets (n_tiles f32, may be NULL), log(1 + measured raster cost).

@@ -94,3 +94,99 @@ def test_trained_network_beats_key_count(renderer):
     assert m["mlp_mae_log"] < m["keycount_mae_log"]
     assert m["mlp_spearman"] > m["keycount_spearman"]
     assert learned.gate(m)
+
+
+@pytest.mark.parametrize("tile,batch", [(16, 0), (32, 256)])
+def test_split_tiles_keep_image_and_costs(renderer, oracle, tile, batch):
+    """Every tile shaded as half-strip items (one pixel a thread) gives the
+    whole-strip image and tile costs bit for bit, under each order."""
+    r = renderer
+    data = scenes.scene_clusters(200_000, seed=7, sh_degree=1)
+    w, h = 1000, 600
+    u = scenes.camera_at((1.0, 2.0, 9.0), w, h).getUniformData(w, h)
+    r.setSplatData(data)
+    r.setTuning(tile, 8, batch)
+    try:
+        out = []
+        for sched in (_lib.SCHEDULE_ROW_MAJOR, _lib.SCHEDULE_KEY_COUNT):
+            r.setSchedule(sched)
+            for split in (False, True):
+                r.setSplitAllTiles(split)
+                r.rebinBatch([(0, u, w, h)])
+                st = r.getScheduleStatus()
+                tiles = r.viewInfo(0).tiles_x * r.viewInfo(0).tiles_y
+                assert st["split_tiles"] == (tiles if split else st["split_tiles"])
+                out.append((r.readViewImage(0).copy(), r.readBuffer("tile_costs")[:tiles].copy()))
+        for img, cost in out[1:]:
+            assert np.array_equal(img.view(np.uint16), out[0][0].view(np.uint16))
+            assert np.array_equal(cost, out[0][1])
+        o = oracle.rebin(u, w, h, tile, tile, data.positions, data.scales, data.rotations,
+                         data.colors, data.sphericalHarmonics, 1)
+        assert np.abs(out[-1][0].astype(np.float32) - o["image"]).max() <= 2.0 / 255.0
+    finally:
+        r.setSplitAllTiles(False)
+        r.setSchedule(_lib.SCHEDULE_ROW_MAJOR)
+        r.setTuning(16, 8, 0)
+
+
+def _install(r, params, mean, std):
+    f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+    params, mean, std = f32(params), f32(mean), f32(std)
+    assert r.lib.gs3d_set_cost_model(r.ctx, params.ctypes.data_as(C.c_void_p),
+                                     mean.ctypes.data_as(C.c_void_p),
+                                     std.ctypes.data_as(C.c_void_p)) == 0
+    r.setSchedule(_lib.SCHEDULE_LEARNED)
+
+
+def test_gate_measures_the_error_and_falls_back(renderer):
+    """The in-library gate on the headline scene: the committed model's
+    measured error stays within its bound and its order is used; a model
+    whose predictions are off by 8 in log cost is measured as such after one
+    frame and the following frames are ordered by key count (same image);
+    reinstalling the good model restores the learned order.  The measured
+    error equals a host computation from the same predictions and costs."""
+    r = renderer
+    data = scenes.scene_clusters(3_000_000, seed=0, sh_degree=3)
+    w, h = 1920, 1080
+    eyes = scenes.orbit_eyes(64, radius=12.0, jitter_deg=20.0, seed=0)
+    us = [scenes.camera_at(eyes[i], w, h).getUniformData(w, h) for i in (3, 17, 40)]
+    r.setSplatData(data)
+    r.setTuning(16, 8, 0)
+    params, mean, std, _, bound = learned.load(learned.checkpoint_for(16, 16))
+    try:
+        r.setScheduleGate(bound)
+        _install(r, params, mean, std)
+        for u in us:
+            r.rebinBatch([(0, u, w, h)])
+        st = r.getScheduleStatus()
+        assert st["frames"] == 3 and st["fallbacks"] == 0
+        assert st["active"] == _lib.SCHEDULE_LEARNED and st["mae_log"] <= bound
+        # the last frame's error from the host: features -> bf16 MLP, recorded costs
+        T = r.viewInfo(0).tiles_x * r.viewInfo(0).tiles_y
+        x = torch.empty((T, 16), device="cuda")
+        t = torch.empty(T, device="cuda")
+        assert r.lib.gs3d_tile_features(r.ctx, dev(x), dev(t), T, 1) == 0
+        assert r.lib.gs3d_synchronize(r.ctx) == 0
+        pred = learned.predict(r.lib, params, mean, std, x)
+        host_mae = float((pred - t).abs().mean())
+        assert abs(st["last_mae_log"] - host_mae) <= 1e-2, (st, host_mae)
+        img_learned = r.readViewImage(0).copy()
+
+        bad = params.copy()
+        bad[-1] += 8.0  # output bias: every prediction 8 too high
+        _install(r, bad, mean, std)
+        r.rebinBatch([(0, us[-1], w, h)])
+        st = r.getScheduleStatus()
+        assert st["active"] == _lib.SCHEDULE_LEARNED and st["last_mae_log"] > 5.0
+        r.rebinBatch([(0, us[-1], w, h)])
+        st = r.getScheduleStatus()
+        assert st["active"] == _lib.SCHEDULE_KEY_COUNT and st["fallbacks"] == 1
+        assert np.array_equal(r.readViewImage(0).view(np.uint16), img_learned.view(np.uint16))
+
+        _install(r, params, mean, std)
+        r.rebinBatch([(0, us[-1], w, h)])
+        r.rebinBatch([(0, us[-1], w, h)])
+        st = r.getScheduleStatus()
+        assert st["active"] == _lib.SCHEDULE_LEARNED and st["fallbacks"] == 0
+    finally:
+        r.setSchedule(_lib.SCHEDULE_ROW_MAJOR)

@@ -88,6 +88,9 @@ struct gs3d_ctx {
   // cost model (learned schedule)
   bool have_model = false;
   DevBuf model_params, model_mean, model_inv_std, tile_feats, tile_preds;
+  DevBuf tile_est;    // expected cost per tile of the last ordered raster
+  DevBuf gate;        // SchedGate: the learned schedule's fallback gate
+  float gate_bound = 0.5f;
 
   // the current batch (a single-view frame is a batch of one)
   bool have_camera = false;
@@ -428,6 +431,7 @@ int set_views(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views, bool upload
   TRY(ensure(c, c->sched_status, sort_status_words((uint32_t)tiles, 4) * 4, "schedule status"));
   TRY(ensure(c, c->tile_feats, std::max<uint64_t>(tiles, 1) * kFeatures * 4, "tile features"));
   TRY(ensure(c, c->tile_preds, std::max<uint64_t>(tiles, 1) * 4, "tile cost predictions"));
+  TRY(ensure(c, c->tile_est, std::max<uint64_t>(tiles, 1) * 4, "tile expected costs"));
   TRY(ensure(c, c->d_views, (size_t)n_views * sizeof(ViewDesc), "view table"));
   if (c->capacity < 1) TRY(ensure_key_capacity(c, 1));
 
@@ -499,9 +503,22 @@ SortPlan tile_digit_plan(uint32_t num_tiles, uint32_t digit_bits) {
 
 int raster_stage(gs3d_ctx* c, bool culled) {
   StageScope t(c, GS3D_STAGE_RASTER);
+  RasterArgs a{};
+  a.views = dviews(c);
+  a.n_views = (uint32_t)c->views.size();
+  a.num_tiles = c->total_tiles;
+  a.tile_w = c->tile_w;
+  a.tile_h = c->tile_h;
+  a.batch = c->raster_batch;
+  a.culled = culled;
+  uint32_t strips = 1, raster_ctas = 1;
+  CK(raster_shape(a, c->sm_count, &strips, &raster_ctas), "raster shape");
+  const bool split_all = (c->flags & GS3D_FLAG_SPLIT_ALL_TILES) != 0;
+  const bool learned = c->schedule == GS3D_SCHEDULE_LEARNED && c->total_tiles > 1;
   const uint32_t* order = nullptr;
+  const uint32_t* heavy = nullptr;
   if (c->schedule != GS3D_SCHEDULE_ROW_MAJOR && c->total_tiles > 1) {
-    if (c->schedule == GS3D_SCHEDULE_LEARNED) {
+    if (learned) {
       const uint32_t nv = (uint32_t)c->views.size();
       CK(launch_tile_features(dviews(c), nv, c->total_tiles, c->tile_w, c->tile_h,
                               u32(c->tile_offsets), u32(c->vals_a),
@@ -515,22 +532,26 @@ int raster_stage(gs3d_ctx* c, bool culled) {
                           static_cast<float*>(c->tile_preds.p), c->stream),
          "cost MLP inference");
       CK(launch_learned_keys(static_cast<float*>(c->tile_preds.p), c->total_tiles,
-                             u32(c->sched_keys_a), u32(c->sched_order_a), c->stream),
+                             static_cast<SchedGate*>(c->gate.p), u32(c->tile_offsets),
+                             u32(c->sched_keys_a), u32(c->sched_order_a),
+                             static_cast<float*>(c->tile_est.p), c->stream),
          "learned schedule keys");
     }
     CK(launch_schedule(c->schedule, u32(c->tile_offsets), c->total_tiles,
-                       &dviews(c)->batch_tiles, u32(c->sched_keys_a), u32(c->sched_order_a), u32(c->sched_keys_b),
-                       u32(c->sched_order_b), u32(c->sched_status), ctrl_of(c), c->sm_count,
-                       c->stream),
+                       &dviews(c)->batch_tiles, u32(c->sched_keys_a), u32(c->sched_order_a),
+                       u32(c->sched_keys_b), u32(c->sched_order_b),
+                       static_cast<float*>(c->tile_est.p), u32(c->sched_status), ctrl_of(c),
+                       raster_ctas, strips, split_all, c->sm_count, c->stream),
        "raster schedule");
     order = u32(c->sched_order_a);
+    heavy = &ctrl_of(c)->raster_heavy;
+  } else if (split_all) {  // row-major order, every tile split
+    CK(launch_heavy_count(nullptr, c->total_tiles, raster_ctas, strips, true,
+                          &ctrl_of(c)->raster_heavy, c->stream),
+       "split all tiles");
+    heavy = &ctrl_of(c)->raster_heavy;
   }
-  RasterArgs a{};
-  a.views = dviews(c);
-  a.n_views = (uint32_t)c->views.size();
-  a.num_tiles = c->total_tiles;
-  a.tile_w = c->tile_w;
-  a.tile_h = c->tile_h;
+  a.heavy = heavy;
   a.proj = static_cast<gs3d_projected_splat*>(c->proj.p);
   a.tile_offsets = u32(c->tile_offsets);
   a.values = u32(c->vals_a);
@@ -549,6 +570,10 @@ int raster_stage(gs3d_ctx* c, bool culled) {
                          cap == cudaStreamCaptureStatusActive ? cudaEventWaitExternal : 0),
      "wait for the previous copy-out");
   CK(launch_raster(a, c->sm_count, c->stream), "rasterize_tiles");
+  if (learned)  // the gate measures this frame's prediction error
+    CK(launch_gate_update(static_cast<float*>(c->tile_preds.p), u32(c->tile_costs),
+                          c->total_tiles, static_cast<SchedGate*>(c->gate.p), c->stream),
+       "schedule gate");
   return GS3D_OK;
 }
 
@@ -792,7 +817,8 @@ int gs3d_destroy(gs3d_ctx* c) {
                     &c->tile_offsets,  &c->image,         &c->tile_costs,    &c->sched_keys_a,
                     &c->sched_keys_b,  &c->sched_order_a, &c->sched_order_b, &c->sched_status,
                     &c->d_views,       &c->ctrl,          &c->model_params,  &c->model_mean,
-                    &c->model_inv_std, &c->tile_feats,    &c->tile_preds,    &c->composite_out};
+                    &c->model_inv_std, &c->tile_feats,    &c->tile_preds,    &c->composite_out,
+                    &c->tile_est,      &c->gate};
   for (DevBuf* b : bufs) release(*b);
   for (int i = 0; i < kUploadSlots; ++i)
     if (c->upload_ev[i]) cudaEventDestroy(c->upload_ev[i]);
@@ -1274,7 +1300,53 @@ int gs3d_set_cost_model(gs3d_ctx* c, const float* params, const float* mean, con
   CK(cudaMemcpy(c->model_params.p, params, kMlpParams * 4, cudaMemcpyHostToDevice), "cost model");
   CK(cudaMemcpy(c->model_mean.p, mean, kFeatures * 4, cudaMemcpyHostToDevice), "cost model");
   CK(cudaMemcpy(c->model_inv_std.p, inv, kFeatures * 4, cudaMemcpyHostToDevice), "cost model");
+  // a new model starts trusted, its running error unmeasured
+  TRY(ensure(c, c->gate, sizeof(SchedGate), "schedule gate"));
+  SchedGate g{};
+  g.bound = c->gate_bound;
+  g.use_learned = 1;
+  CK(cudaMemcpy(c->gate.p, &g, sizeof(g), cudaMemcpyHostToDevice), "schedule gate");
   c->have_model = true;
+  return GS3D_OK;
+}
+
+int gs3d_set_schedule_gate(gs3d_ctx* c, float bound) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  if (!(bound >= 0.0f)) return fail(c, GS3D_ERR_INVALID_ARG, "gate bound must be >= 0");
+  TRY(set_device(c));
+  c->gate_bound = bound;
+  if (c->gate.p) {  // stream ordered with the rebins that read it
+    CK(cudaMemcpyAsync(&static_cast<SchedGate*>(c->gate.p)->bound, &c->gate_bound,
+                       sizeof(float), cudaMemcpyHostToDevice, c->stream),
+       "schedule gate");
+    CK(cudaStreamSynchronize(c->stream), "schedule gate");
+  }
+  return GS3D_OK;
+}
+
+int gs3d_get_schedule_status(gs3d_ctx* c, gs3d_schedule_status* out) {
+  if (!c || !out) return fail(c, GS3D_ERR_INVALID_ARG, "null argument");
+  TRY(set_device(c));
+  TRY(sync_and_check(c));
+  *out = gs3d_schedule_status{};
+  out->schedule = c->schedule;
+  out->active = c->schedule;
+  out->bound = c->gate_bound;
+  if (c->gate.p) {
+    SchedGate g{};
+    CK(cudaMemcpy(&g, c->gate.p, sizeof(g), cudaMemcpyDeviceToHost), "schedule gate");
+    out->mae_log = g.mae;
+    out->last_mae_log = g.last_mae;
+    out->frames = g.frames;
+    out->fallbacks = g.fallbacks;
+    if (c->schedule == GS3D_SCHEDULE_LEARNED && g.frames > 0 && !g.used_learned)
+      out->active = GS3D_SCHEDULE_KEY_COUNT;
+  }
+  if (c->ctrl.p) {
+    CK(cudaMemcpy(&out->split_tiles, &ctrl_of(c)->raster_heavy, sizeof(uint32_t),
+                  cudaMemcpyDeviceToHost),
+       "split tiles");
+  }
   return GS3D_OK;
 }
 

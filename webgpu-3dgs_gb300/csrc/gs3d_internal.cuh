@@ -86,10 +86,24 @@ struct Ctrl {
   uint32_t sort_part_counter[kMaxSortPasses];
   uint32_t raster_queue;
   uint32_t sched_counter[2];
-  uint32_t pad[3];
+  uint32_t raster_heavy;  // tiles at the head of the raster order shaded as half strips
+  uint32_t pad[2];
   uint32_t sort_hist[kMaxSortPasses][kRadixBins];  // global digit histograms
   uint32_t sched_hist[2][kRadixBins];
   uint32_t tile_hist[kMaxTilePasses][kTileHistStride];  // fused rebin's tile passes
+};
+
+// Fallback gate of the learned raster schedule, kept on the device across
+// frames (set by gs3d_set_cost_model, updated after every learned raster).
+struct SchedGate {
+  float bound;            // largest running error at which the learned order is used
+  float mae;              // running mean |predicted - measured log(1 + cost)|
+  float last_mae;         // the last frame's
+  uint32_t frames;        // frames measured
+  uint32_t use_learned;   // order of the next frame: 1 learned, 0 key count
+  uint32_t used_learned;  // order of the last frame
+  uint32_t fallbacks;     // frames rendered in key-count order by the gate
+  uint32_t pad;
 };
 
 // Bounded spins: a device wait gives up after this many polls (with
@@ -293,12 +307,22 @@ cudaError_t launch_sort_depth_keys(const uint32_t* count, uint32_t capacity, uin
 // Raster work order: tile indices sorted by decreasing expected cost
 // (schedule = GS3D_SCHEDULE_KEY_COUNT: the tile's key count), so the
 // persistent raster CTAs start the longest tiles first.
-// keys_a/order_a must already hold the keys for GS3D_SCHEDULE_LEARNED
-// (launch_learned_keys); for the key-count schedule they are computed here.
+// keys_a/order_a and est (the expected cost of every tile) must already be
+// written for GS3D_SCHEDULE_LEARNED (launch_learned_keys); for the key-count
+// schedule they are computed here.  Also sets ctrl->raster_heavy
+// (launch_heavy_count).
 cudaError_t launch_schedule(uint32_t schedule, const uint32_t* tile_offsets, uint32_t num_tiles,
                             const uint32_t* num_tiles_dev, uint32_t* keys_a, uint32_t* order_a,
-                            uint32_t* keys_b, uint32_t* order_b, uint32_t* status, Ctrl* ctrl,
+                            uint32_t* keys_b, uint32_t* order_b, float* est, uint32_t* status,
+                            Ctrl* ctrl, uint32_t raster_ctas, uint32_t strips, bool split_all,
                             int sm_count, cudaStream_t s);
+// The per-tile split: *heavy = the number of tiles (the head of an order by
+// decreasing est) whose expected cost per strip exceeds half of one raster
+// CTA's fair share of the frame, sum(est) * strips / raster_ctas; those tiles
+// are shaded as two half-strip work items per strip.  all: every tile (est
+// may be null).
+cudaError_t launch_heavy_count(const float* est, uint32_t n, uint32_t raster_ctas,
+                               uint32_t strips, bool all, uint32_t* heavy, cudaStream_t s);
 
 // ---- learned schedule (learned.cu) ----
 constexpr int kFeatures = 16;
@@ -317,8 +341,15 @@ cudaError_t launch_mlp_backward(const float* params, const float* x, const float
                                 const float* target, uint32_t n, float* grads, cudaStream_t s);
 cudaError_t launch_adam(float* p, float* m, float* v, const float* g, uint32_t count, float lr,
                         float beta1, float beta2, float eps, uint32_t step, cudaStream_t s);
-cudaError_t launch_learned_keys(const float* pred, uint32_t n, uint32_t* keys, uint32_t* ids,
-                                cudaStream_t s);
+// Schedule keys (decreasing expected cost first) and expected costs: from the
+// cost MLP's predictions while gate->use_learned, else from the key counts.
+cudaError_t launch_learned_keys(const float* pred, uint32_t n, const SchedGate* gate,
+                                const uint32_t* tile_offsets, uint32_t* keys, uint32_t* ids,
+                                float* est, cudaStream_t s);
+// After a learned raster: the frame's mean |pred - log(1 + cost)| over tiles
+// updates the gate's running error and its choice for the next frame.
+cudaError_t launch_gate_update(const float* pred, const uint32_t* costs, uint32_t n,
+                               SchedGate* gate, cudaStream_t s);
 cudaError_t launch_log_costs(const uint32_t* costs, uint32_t n, float* out, cudaStream_t s);
 
 // Emit in depth-sorted order over all splat-views of a batch (global tile
@@ -354,8 +385,14 @@ struct RasterArgs {
   uint32_t batch;         // splats staged per batch (0 = tile_w * tile_h)
   bool culled;
   uint32_t split;         // CTAs per tile (row strips), set by launch_raster
+  // tiles at the head of the order shaded as two half-strip items per strip
+  // (device count, two-pixel culled variant only; may be null: none)
+  const uint32_t* heavy;
 };
 cudaError_t launch_raster(const RasterArgs& a, int sm_count, cudaStream_t s);
+// Row strips per tile and resident CTAs of the raster launch for these args.
+cudaError_t raster_shape(const RasterArgs& a, int sm_count, uint32_t* strips,
+                         uint32_t* resident_ctas);
 
 // Headless composite of one view's splat target over a background colour,
 // optionally through the tile heat-map overlay; out = W*H RGBA8 words.

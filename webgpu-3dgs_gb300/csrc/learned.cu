@@ -367,15 +367,60 @@ __global__ void log_costs_kernel(const uint32_t* __restrict__ costs, uint32_t n,
   if (t < n) out[t] = log1pf((float)costs[t]);
 }
 
-// Schedule keys from predictions: larger predicted cost first.
+// Schedule keys: larger expected cost first.  While the gate accepts the
+// model the expected cost is its prediction, else the key count (the
+// key-count schedule's keys).
 __global__ void learned_keys_kernel(const float* __restrict__ pred, uint32_t n,
-                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ ids) {
+                                    const SchedGate* __restrict__ gate,
+                                    const uint32_t* __restrict__ tile_offsets,
+                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ ids,
+                                    float* __restrict__ est) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
-  // pred = log(1 + cost); 4096 steps per unit of log cost, 16-bit key
-  const float c = fminf(fmaxf(pred[t], 0.0f), 15.99f);
-  keys[t] = 0xffffu - (uint32_t)(c * 4096.0f);
+  if (gate->use_learned) {
+    // pred = log(1 + cost); 4096 steps per unit of log cost, 16-bit key
+    const float c = fminf(fmaxf(pred[t], 0.0f), 15.99f);
+    keys[t] = 0xffffu - (uint32_t)(c * 4096.0f);
+    est[t] = expm1f(c);
+  } else {
+    const uint32_t lo = __ldg(tile_offsets + t), hi = __ldg(tile_offsets + t + 1);
+    const uint32_t k = hi > lo ? hi - lo : 0u;
+    keys[t] = 0xffffu - min(k, 0xffffu);
+    est[t] = (float)k;
+  }
   ids[t] = t;
+}
+
+// One block: the frame's mean |pred - log(1 + cost)| over all tiles (fixed
+// reduction order), folded into the running error (weight 1/4 per frame,
+// the first frame taken as is); the learned order stays in use while the
+// running error is within the bound.
+constexpr int kGateThreads = 1024;
+__global__ void __launch_bounds__(kGateThreads)
+    gate_update_kernel(const float* __restrict__ pred, const uint32_t* __restrict__ costs,
+                       uint32_t n, SchedGate* __restrict__ gate) {
+  __shared__ float s_sum[kGateThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float sum = 0.0f;
+  for (uint32_t t = threadIdx.x; t < n; t += kGateThreads)
+    sum += fabsf(pred[t] - log1pf((float)costs[t]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (lane == 0) s_sum[warp] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float total = 0.0f;
+    for (int w = 0; w < kGateThreads / 32; ++w) total += s_sum[w];
+    const float mae = n ? total / (float)n : 0.0f;
+    SchedGate g = *gate;
+    g.last_mae = mae;
+    g.mae = g.frames == 0 ? mae : 0.75f * g.mae + 0.25f * mae;
+    g.frames += 1;
+    g.used_learned = g.use_learned;
+    if (!g.use_learned) g.fallbacks += 1;
+    g.use_learned = g.mae <= g.bound ? 1u : 0u;
+    *gate = g;
+  }
 }
 
 }  // namespace
@@ -429,10 +474,18 @@ cudaError_t launch_log_costs(const uint32_t* costs, uint32_t n, float* out, cuda
   return cudaGetLastError();
 }
 
-cudaError_t launch_learned_keys(const float* pred, uint32_t n, uint32_t* keys, uint32_t* ids,
-                                cudaStream_t s) {
+cudaError_t launch_learned_keys(const float* pred, uint32_t n, const SchedGate* gate,
+                                const uint32_t* tile_offsets, uint32_t* keys, uint32_t* ids,
+                                float* est, cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  learned_keys_kernel<<<(n + 255) / 256, 256, 0, s>>>(pred, n, keys, ids);
+  learned_keys_kernel<<<(n + 255) / 256, 256, 0, s>>>(pred, n, gate, tile_offsets, keys, ids,
+                                                       est);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gate_update(const float* pred, const uint32_t* costs, uint32_t n,
+                               SchedGate* gate, cudaStream_t s) {
+  gate_update_kernel<<<1, kGateThreads, 0, s>>>(pred, costs, n, gate);
   return cudaGetLastError();
 }
 

@@ -367,19 +367,23 @@ __device__ void raster_tile_plain(const RasterArgs& a, const TileGeom& g, SplatS
 // Culled variant: warps own compact pixel blocks and skip splats that no
 // pixel of their block can blend.  blockDim.x == tile_w * tile_h, a multiple
 // of 32.
-__device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, SplatStage* buf0,
-                                   SplatStage* buf1, uint32_t* s_cost) {
+// The tile's rows [row0, row0 + nthr / tile_w) are shaded by the CTA's nthr
+// threads, one pixel each (the whole tile in the one-pixel kernel; half a
+// row strip when the two-pixel kernel splits a heavy tile).
+__device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, uint32_t row0,
+                                   uint32_t nthr, SplatStage* buf0, SplatStage* buf1,
+                                   uint32_t* s_cost) {
   const uint32_t nt = a.tile_w * a.tile_h;
   const uint32_t D = a.batch ? a.batch : nt;  // splats per staged batch
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   uint32_t lx, ly;
-  if ((a.tile_w % 8 == 0) && (a.tile_h % 4 == 0)) {  // 8x4 pixel block per warp
+  if ((a.tile_w % 8 == 0) && ((nthr / a.tile_w) % 4 == 0)) {  // 8x4 pixel block per warp
     const uint32_t bw = a.tile_w / 8;
     lx = (warp % bw) * 8 + (lane & 7);
-    ly = (warp / bw) * 4 + (lane >> 3);
+    ly = row0 + (warp / bw) * 4 + (lane >> 3);
   } else {
     lx = tid % a.tile_w;
-    ly = tid / a.tile_w;
+    ly = row0 + tid / a.tile_w;
   }
   const uint32_t px = g.ox + lx;
   const uint32_t py = g.oy + ly;
@@ -404,17 +408,17 @@ __device__ void raster_tile_culled(const RasterArgs& a, const TileGeom& g, Splat
   bool done = !in_bounds;
   uint32_t used = 0;
 
-  if (nbatches > 0) stage_batch(a.proj, a.values, start, end, D, nt, buf0);
+  if (nbatches > 0) stage_batch(a.proj, a.values, start, end, D, nthr, buf0);
   for (uint32_t bi = 0; bi < nbatches; ++bi) {
     SplatStage* cur = (bi & 1) ? buf1 : buf0;
     if (bi + 1 < nbatches) {
-      stage_batch(a.proj, a.values, start + (bi + 1) * D, end, D, nt, (bi & 1) ? buf0 : buf1);
+      stage_batch(a.proj, a.values, start + (bi + 1) * D, end, D, nthr, (bi & 1) ? buf0 : buf1);
       cp_async_wait<1>();
     } else {
       cp_async_wait<0>();
     }
     const uint32_t cnt = min(D, end - (start + bi * D));
-    for (uint32_t k = tid; k < cnt; k += nt) prepare(cur[k]);  // own copies are complete
+    for (uint32_t k = tid; k < cnt; k += nthr) prepare(cur[k]);  // own copies are complete
     __syncthreads();
     if (__any_sync(0xffffffffu, !done)) {
       for (uint32_t k0 = 0; k0 < cnt; k0 += 32) {
@@ -561,6 +565,11 @@ __device__ __forceinline__ void raster_loop(const RasterArgs& a) {
   SplatStage* buf0 = reinterpret_cast<SplatStage*>(smem);
   SplatStage* buf1 = buf0 + D;
   __shared__ uint32_t s_item, s_cost;
+  // work items: the first `heavy` tiles of the order as two half-strip items
+  // per strip, then one item per strip of the others
+  const uint32_t heavy = (MODE == 2 && a.heavy != nullptr) ? min(__ldg(a.heavy), a.num_tiles) : 0u;
+  const uint32_t heavy_items = 2u * a.split * heavy;
+  const uint32_t items = heavy_items + (a.num_tiles - heavy) * a.split;
   while (true) {
     if (threadIdx.x == 0) {
       s_item = atomicAdd(a.queue_counter, 1u);
@@ -568,23 +577,37 @@ __device__ __forceinline__ void raster_loop(const RasterArgs& a) {
     }
     __syncthreads();
     const uint32_t item = s_item;
-    if (item >= a.num_tiles * a.split) break;
-    const uint32_t ti = item / a.split, strip = item - ti * a.split;
+    if (item >= items) break;
+    uint32_t ti, strip, half;  // half: 0 whole strip, 1 / 2 first / second half
+    if (item < heavy_items) {
+      ti = item / (2u * a.split);
+      const uint32_t sub = item - ti * 2u * a.split;
+      strip = sub >> 1;
+      half = 1u + (sub & 1u);
+    } else {
+      const uint32_t j = item - heavy_items;
+      ti = heavy + j / a.split;
+      strip = j - (ti - heavy) * a.split;
+      half = 0u;
+    }
     const uint32_t t = a.order != nullptr ? __ldg(a.order + ti) : ti;
     const TileGeom g = tile_geom(a, t);
-    if (MODE == 2)
-      raster_tile_culled2(a, g, strip, buf0, buf1, &s_cost);
-    else if (MODE == 1)
-      raster_tile_culled(a, g, buf0, buf1, &s_cost);
-    else
+    if (MODE == 2) {
+      if (half == 0u) {
+        raster_tile_culled2(a, g, strip, buf0, buf1, &s_cost);
+      } else {  // half a row strip, one pixel a thread (the same per-pixel arithmetic)
+        const uint32_t strip_h = a.tile_h / a.split;
+        raster_tile_culled(a, g, strip * strip_h + (half - 1u) * (strip_h / 2), blockDim.x, buf0,
+                           buf1, &s_cost);
+      }
+    } else if (MODE == 1) {
+      raster_tile_culled(a, g, 0u, a.tile_w * a.tile_h, buf0, buf1, &s_cost);
+    } else {
       raster_tile_plain(a, g, buf0, buf1, &s_cost);
-    __syncthreads();  // s_cost complete; shared buffers free for the next tile
-    if (threadIdx.x == 0 && a.tile_costs != nullptr) {
-      if (a.split == 1)
-        a.tile_costs[t] = s_cost;
-      else
-        atomicMax(a.tile_costs + t, s_cost);  // zeroed before the launch
     }
+    __syncthreads();  // s_cost complete; shared buffers free for the next tile
+    if (threadIdx.x == 0 && a.tile_costs != nullptr)
+      atomicMax(a.tile_costs + t, s_cost);  // zeroed before the launch; max over a tile's items
   }
 }
 
@@ -595,11 +618,16 @@ __global__ void __launch_bounds__(512, 2) raster_kernel_culled2(RasterArgs a) {
   raster_loop<2>(a);
 }
 
-}  // namespace
+// Variant, strips, block size, staged batch and resident CTAs per SM of the
+// raster launch for `a` (the occupancy is computed once per device and shape).
+struct RasterConfig {
+  int mode;
+  uint32_t split, threads, D;
+  int per_sm;
+  void (*kern)(RasterArgs);
+};
 
-cudaError_t launch_raster(const RasterArgs& args, int sm_count, cudaStream_t s) {
-  if (args.num_tiles == 0) return cudaSuccess;
-  RasterArgs a = args;
+cudaError_t raster_config(const RasterArgs& a, RasterConfig* cfg) {
   const uint32_t nt = a.tile_w * a.tile_h;
   if (a.batch % 32 != 0 || a.batch > 1024) return cudaErrorInvalidValue;
   const uint32_t D = a.batch ? a.batch : nt;
@@ -609,14 +637,9 @@ cudaError_t launch_raster(const RasterArgs& args, int sm_count, cudaStream_t s) 
   // two-pixel tiles of more than 512 pixels are shaded by four (else two)
   // CTAs of row strips whose heights divide by 8, so that a block barrier
   // waits for few warps and more CTAs interleave on an SM
-  a.split = 1;
-  if (mode == 2 && nt > 512) a.split = (a.tile_h / 4) % 8 == 0 ? 4u : (a.tile_h / 2) % 8 == 0 ? 2u : 1u;
-  const uint32_t threads = mode == 2 ? nt / (2 * a.split) : nt;
-  if (a.split > 1 && a.tile_costs != nullptr) {
-    const cudaError_t e =
-        cudaMemsetAsync(a.tile_costs, 0, (size_t)a.num_tiles * sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
-  }
+  uint32_t split = 1;
+  if (mode == 2 && nt > 512) split = (a.tile_h / 4) % 8 == 0 ? 4u : (a.tile_h / 2) % 8 == 0 ? 2u : 1u;
+  const uint32_t threads = mode == 2 ? nt / (2 * split) : nt;
   const size_t smem = 2 * (size_t)D * sizeof(SplatStage);
   auto kern = mode == 2 ? raster_kernel_culled2 : mode == 1 ? raster_kernel_culled
                                                              : raster_kernel_plain;
@@ -650,9 +673,40 @@ cudaError_t launch_raster(const RasterArgs& args, int sm_count, cudaStream_t s) 
     std::lock_guard<std::mutex> lock(mu);
     cache[key] = per_sm;
   }
+  *cfg = RasterConfig{mode, split, threads, D, per_sm, kern};
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t raster_shape(const RasterArgs& a, int sm_count, uint32_t* strips,
+                         uint32_t* resident_ctas) {
+  RasterConfig cfg;
+  const cudaError_t e = raster_config(a, &cfg);
+  if (e != cudaSuccess) return e;
+  *strips = cfg.split;
+  *resident_ctas = (uint32_t)sm_count * (uint32_t)cfg.per_sm;
+  return cudaSuccess;
+}
+
+cudaError_t launch_raster(const RasterArgs& args, int sm_count, cudaStream_t s) {
+  if (args.num_tiles == 0) return cudaSuccess;
+  RasterArgs a = args;
+  RasterConfig cfg;
+  cudaError_t e = raster_config(a, &cfg);
+  if (e != cudaSuccess) return e;
+  a.split = cfg.split;
+  if (cfg.mode != 2) a.heavy = nullptr;  // half strips exist in the two-pixel variant only
+  // every work item folds its cost into its tile's by maximum
+  if (a.tile_costs != nullptr) {
+    e = cudaMemsetAsync(a.tile_costs, 0, (size_t)a.num_tiles * sizeof(uint32_t), s);
+    if (e != cudaSuccess) return e;
+  }
+  // up to two items per strip when tiles are split
+  const uint64_t max_items = (uint64_t)a.num_tiles * a.split * (a.heavy != nullptr ? 2 : 1);
   const uint32_t grid = (uint32_t)std::min<uint64_t>(
-      (uint64_t)a.num_tiles * a.split, (uint64_t)sm_count * (uint64_t)std::max(per_sm, 1));
-  kern<<<grid, threads, smem, s>>>(a);
+      max_items, (uint64_t)sm_count * (uint64_t)std::max(cfg.per_sm, 1));
+  cfg.kern<<<grid, cfg.threads, 2 * (size_t)cfg.D * sizeof(SplatStage), s>>>(a);
   return cudaGetLastError();
 }
 

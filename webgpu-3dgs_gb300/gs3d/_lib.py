@@ -29,6 +29,7 @@ STATUS_NAMES = {
 FLAG_STAGEWISE_REBIN = 1
 FLAG_STAGE_TIMING = 2
 FLAG_CUDA_GRAPH = 4
+FLAG_SPLIT_ALL_TILES = 8
 STAGE_NAMES = ["preprocess-splats", "depth-sort", "prefix-scan", "emit-tile-refs", "radix-sort",
                "identify-tile-ranges", "rasterize-tiles"]
 
@@ -97,6 +98,14 @@ class ViewInfo_t(C.Structure):
 SCHEDULE_ROW_MAJOR = 0
 SCHEDULE_KEY_COUNT = 1
 SCHEDULE_LEARNED = 2
+
+
+class ScheduleStatus_t(C.Structure):
+    _fields_ = [("schedule", C.c_uint32), ("active", C.c_uint32), ("mae_log", C.c_float),
+                ("last_mae_log", C.c_float), ("bound", C.c_float), ("frames", C.c_uint32),
+                ("fallbacks", C.c_uint32), ("split_tiles", C.c_uint32)]
+
+
 MLP_FEATURES, MLP_HIDDEN = 16, 64
 MLP_PARAMS = 64 * 16 + 64 + 64 * 64 + 64 + 64 + 1
 
@@ -142,6 +151,8 @@ SIGNATURES = {
     "gs3d_composite": ([_P, _U32, _U32, _U32, _P, _P, _SZ, _I], _I),
     "gs3d_load_ply": ([_P, _P, _SZ, _U32, C.POINTER(_U32), C.POINTER(PlyInfo_t)], _I),
     "gs3d_set_cost_model": ([_P, _P, _P, _P], _I),
+    "gs3d_set_schedule_gate": ([_P, C.c_float], _I),
+    "gs3d_get_schedule_status": ([_P, C.POINTER(ScheduleStatus_t)], _I),
     "gs3d_tile_features": ([_P, _P, _P, _U32, _I], _I),
     "gs3d_mlp_forward": ([_P, _P, _U32, _P, _P, _P], _I),
     "gs3d_mlp_backward": ([_P, _P, _P, _P, _U32, _P, _P], _I),

@@ -155,7 +155,10 @@ class GaussianSplatRenderer:
         1080p workload).  When its held-out error is within its bound and it
         ranks tiles better than the key count, it is installed and the learned
         schedule selected; otherwise the key-count schedule is selected.
-        Returns whether the learned schedule is active."""
+        Once installed, the library measures the model's error against the
+        costs every raster records and orders frames by key count while the
+        running error exceeds the checkpoint's bound (getScheduleStatus).
+        Returns whether the learned schedule is selected."""
         from pathlib import Path
         from . import learned
         path = Path(path) if path else Path(__file__).with_name("cost_mlp_c1.npz")
@@ -165,10 +168,30 @@ class GaussianSplatRenderer:
             return False
         f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
         params, mean, std = f32(params), f32(mean), f32(std)
+        self.setScheduleGate(bound)
         self._call("gs3d_set_cost_model", params.ctypes.data_as(C.c_void_p),
                    mean.ctypes.data_as(C.c_void_p), std.ctypes.data_as(C.c_void_p))
         self.setSchedule(_lib.SCHEDULE_LEARNED)
         return True
+
+    def setScheduleGate(self, bound: float) -> None:
+        """Bound on the learned schedule's running mean |log cost error|; above
+        it the library orders frames by key count until the error recovers."""
+        self._call("gs3d_set_schedule_gate", float(bound))
+
+    def getScheduleStatus(self) -> dict:
+        """Requested and active raster order, the gate's measured error and
+        the number of tiles the last raster split (blocking)."""
+        st = _lib.ScheduleStatus_t()
+        self._call("gs3d_get_schedule_status", C.byref(st))
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def setSplitAllTiles(self, on: bool) -> None:
+        """Shades every tile as half-strip work items (testing the split; the
+        image is unchanged)."""
+        self._flags = (getattr(self, "_flags", 0) & ~_lib.FLAG_SPLIT_ALL_TILES) | \
+            (_lib.FLAG_SPLIT_ALL_TILES if on else 0)
+        self._call("gs3d_set_flags", self._flags)
 
     def setTuning(self, tile: int | tuple[int, int] = 16, digit_bits: int = 8,
                   raster_batch: int = 0) -> None:
