@@ -1430,7 +1430,8 @@ int gs3d_read_stage_times(gs3d_ctx* c, double* ms, uint32_t* n) {
 
 int gs3d_set_flags(gs3d_ctx* c, uint32_t flags) {
   if (!c) return GS3D_ERR_INVALID_ARG;
-  if (flags & ~(GS3D_FLAG_STAGEWISE_REBIN | GS3D_FLAG_STAGE_TIMING | GS3D_FLAG_CUDA_GRAPH))
+  if (flags & ~(GS3D_FLAG_STAGEWISE_REBIN | GS3D_FLAG_STAGE_TIMING | GS3D_FLAG_CUDA_GRAPH |
+                GS3D_FLAG_SPLIT_ALL_TILES))
     return fail(c, GS3D_ERR_INVALID_ARG, "unknown flag bits 0x%x", flags);
   c->flags = flags;
   return GS3D_OK;
