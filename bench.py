@@ -384,12 +384,21 @@ def run_ours(args, rank, world):
         return total, per_stage, clocks.summary()
 
     views = args.steps * len(cam_structs)
-    # headline: batched, autotuned, learned schedule, CUDA graph replays
-    batched_ms, _, clocks = timed("batched", batched_schedule, graph=True)
+    # headline: batched, autotuned, CUDA graph replays, under each raster
+    # order (the same image); the headline value is the fastest order's
+    orders = [("row_major", _lib.SCHEDULE_ROW_MAJOR), ("key_count", _lib.SCHEDULE_KEY_COUNT)]
+    if batched_schedule == _lib.SCHEDULE_LEARNED:
+        orders.append(("learned", _lib.SCHEDULE_LEARNED))
+    graph_runs = {}
+    for name, sc in orders:
+        ms_, _, clk = timed("batched", sc, graph=True)
+        graph_runs[name] = (ms_, clk, sc)
+    best_order = min(graph_runs, key=lambda k: graph_runs[k][0])
+    batched_ms, clocks, best_sched = graph_runs[best_order]
     # the same path, each batch bracketed by its own events: the median over
     # steps x batches samples (the reference's timing protocol)
     check(lib.gs3d_set_flags(ctx, _lib.FLAG_CUDA_GRAPH))
-    check(lib.gs3d_set_schedule(ctx, batched_schedule))
+    check(lib.gs3d_set_schedule(ctx, best_sched))
     run_step("batched")
     check(lib.gs3d_synchronize(ctx))
     marks = []
@@ -407,14 +416,15 @@ def run_ours(args, rank, world):
                     "views_per_s": round(1e3 / statistics.median(per_view_ms), 1),
                     "samples": len(per_view_ms)}
     check(lib.gs3d_set_flags(ctx, 0))
-    eager_ms, batched_stages, _ = timed("batched", batched_schedule)  # per-stage events
-    # the raster under each work order on the tuned batched path (same image)
+    eager_ms, batched_stages, _ = timed("batched", best_sched)  # per-stage events
+    # each work order on the tuned batched path (same image): graph-replay
+    # views/s and the raster's eager per-stage time
     sched_batched = {}
-    for name, sc in (("row_major", _lib.SCHEDULE_ROW_MAJOR), ("key_count", _lib.SCHEDULE_KEY_COUNT),
-                     ("learned", batched_schedule)):
+    for name, sc in orders:
         ms_, st_, _ = timed("batched", sc)
         sched_batched[name] = {"raster_ms": round(st_["rasterize-tiles"][0], 4),
-                               "views_per_s": round(views * world / (ms_ * 1e-3), 1)}
+                               "views_per_s": round(views * world / (graph_runs[name][0] * 1e-3),
+                                                    1)}
 
     # ---- e2e: the public batched entry point with host view tables in and
     # pinned host images out, every batch, under the same tuning ----
@@ -422,7 +432,7 @@ def run_ours(args, rank, world):
     batch_bytes = img_bytes * B
     pinned = torch.empty(batch_bytes * 2, dtype=torch.uint8, pin_memory=True)
     check(lib.gs3d_set_flags(ctx, _lib.FLAG_CUDA_GRAPH))
-    check(lib.gs3d_set_schedule(ctx, batched_schedule))
+    check(lib.gs3d_set_schedule(ctx, best_sched))
     for _ in range(2):  # warm-up: graph capture, and first copies into both pinned slots
         for bi, arr in enumerate(batches):
             check(lib.gs3d_rebin_batch(ctx, C.cast(arr, C.c_void_p), len(arr)))
@@ -513,9 +523,12 @@ def run_ours(args, rank, world):
     dom = max(hbm, key=lambda s: batched_roof[s]["ms"])
     learned_on = batched_schedule == _lib.SCHEDULE_LEARNED
     # kernels of one batched rebin: preprocess, depth sort (histogram + 4 passes), scan, emit,
-    # tile-digit passes, identify, schedule (features + MLP + keys + histogram + 2 passes
-    # for the learned one; keys + histogram + 2 passes for key counts), raster
-    launches_per_batch = 1 + 5 + 1 + 1 + tuned_passes + 1 + (6 if learned_on else 4) + 1
+    # tile-digit passes, identify, schedule (features + MLP + keys + split count + histogram
+    # + 2 passes + gate for the learned order; keys + split count + histogram + 2 passes for
+    # key counts; none for row-major), raster
+    sched_kernels = {_lib.SCHEDULE_ROW_MAJOR: 0, _lib.SCHEDULE_KEY_COUNT: 5,
+                     _lib.SCHEDULE_LEARNED: 8}[best_sched]
+    launches_per_batch = 1 + 5 + 1 + 1 + tuned_passes + 1 + sched_kernels + 1
     return {
         "value": views * world / (batched_ms * 1e-3), "ms_per_step": batched_ms / args.steps,
         "views": views, "per_stage": batched_roof, "dominant": dom, "peak": peak,
@@ -532,7 +545,7 @@ def run_ours(args, rank, world):
         "h2d": 416 * len(cam_structs), "d2h": img_bytes * len(cam_structs),
         "launches_per_step": launches_per_batch * len(batches),
         "schedules": sched_raster, "schedules_batched": sched_batched,
-        "learned_active": learned_on,
+        "learned_active": learned_on, "best_order": best_order,
         "cost_model": {k: round(v, 4) for k, v in (tuned_model or {}).items()},
         "tuning": {"tile": tuned.tile_w, "digit_bits": tuned.digit_bits,
                    "raster_batch": tuned.raster_batch, "candidates": tune_table},
@@ -547,6 +560,178 @@ def run_ours(args, rank, world):
             "reference_8_pass_16x16": int(8 * mean_R + 8 * 24 * mean_R),
             "this_path": int(4 * N_SPLATS + 4 * 16 * N_SPLATS + tuned_passes * 24 * tuned_R)},
     }
+
+
+SIZES_C2 = [(640, 360), (1280, 720), (1920, 1080), (2560, 1440), (3840, 2160)]
+
+
+def c2_workload():
+    """The batched configuration: 4 scenes of 0.5M, 1M, 3M and 6M splats
+    (cluster distribution, seeds 1-4, SH 3) and one batch of 32 views at sizes
+    drawn from 640x360 ... 3840x2160, random poses at radius 8-16."""
+    from gs3d import scenes
+    scs = [scenes.scene_clusters(n, seed=s, sh_degree=3)
+           for n, s in ((500_000, 1), (1_000_000, 2), (3_000_000, 3), (6_000_000, 4))]
+    rng = np.random.default_rng(11)
+    eyes = scenes.random_eyes(32, 8.0, 16.0, seed=11)
+    views = []
+    for i in range(32):
+        w, h = SIZES_C2[int(rng.integers(len(SIZES_C2)))]
+        views.append((i % 4, scenes.camera_at(eyes[i], w, h).getUniformData(w, h), w, h))
+    return scs, [views]
+
+
+def c4_workload():
+    """The skewed stress configuration: 10M splats (16 dense clusters + 20%
+    background, heavy-tailed scales, SH 3), 8 close-up and 8 wide 3840x2160
+    views; batches of 2 close-ups (about 1.1e9 refs each at 32x32 tiles) and
+    one batch of the 8 wide views, within one rebin's 2^32 refs."""
+    from gs3d import scenes
+    data = scenes.scene_skewed(10_000_000, seed=0, sh_degree=3)
+    W, H = 3840, 2160
+    close = scenes.random_eyes(8, 3.0, 5.0, seed=21)
+    wide = scenes.random_eyes(8, 28.0, 34.0, seed=22)
+    cv = [(0, scenes.camera_at(e, W, H).getUniformData(W, H), W, H) for e in close]
+    wv = [(0, scenes.camera_at(e, W, H).getUniformData(W, H), W, H) for e in wide]
+    return [data], [cv[0:2], cv[2:4], cv[4:6], cv[6:8], wv]
+
+
+def run_extra_config(name, scenes_data, batches, tuning, steps, warmup):
+    """views/s of one configuration under the batched path (CUDA-graph replay)
+    with each raster order, and of the plain single-view path (fused rebin,
+    16x16 tiles, row-major), with per-stage times and the learned order's
+    gate state.  Every step renders every view once."""
+    import torch
+
+    from gs3d import _lib
+    from gs3d.camera import camera_struct
+
+    lib = _lib.load()
+    stream = torch.cuda.Stream()
+    ctx = C.c_void_p()
+    cfg = _lib.Config_t(int(os.environ.get("LOCAL_RANK", 0)), 16, 16, 16,
+                        C.c_void_p(stream.cuda_stream), 0)
+    if lib.gs3d_create(C.byref(ctx), C.byref(cfg)) != 0:
+        raise RuntimeError("gs3d_create failed")
+
+    def check(rc):
+        if rc != 0:
+            raise RuntimeError(f"{name}: " + lib.gs3d_last_error(ctx).decode())
+
+    ptr = lambda a: None if a is None else a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    for i, d in enumerate(scenes_data):
+        args = (d.splatCount, ptr(d.positions), ptr(d.scales), ptr(d.rotations), ptr(d.colors),
+                ptr(d.sphericalHarmonics), d.sphericalHarmonicsDegree, 0)
+        if i == 0:
+            check(lib.gs3d_set_splats(ctx, *args))
+        else:
+            sid = C.c_uint32()
+            check(lib.gs3d_add_scene(ctx, *args, C.byref(sid)))
+    arrs = []
+    for vs in batches:
+        arr = (_lib.View_t * len(vs))()
+        for i, (sid, u, w, h) in enumerate(vs):
+            arr[i].camera = camera_struct(u)
+            arr[i].scene, arr[i].width, arr[i].height = sid, w, h
+        arrs.append(arr)
+    n_views = sum(len(a) for a in arrs)
+    if tuning is None:  # autotune on the first batch
+        out = (_lib.TuneResult_t * 64)()
+        n = C.c_uint32()
+        check(lib.gs3d_autotune(ctx, C.cast(arrs[0], C.c_void_p), len(arrs[0]), 1, out, 64,
+                                C.byref(n)))
+    else:
+        check(lib.gs3d_set_tuning(ctx, C.byref(_lib.Tuning_t(*tuning))))
+    tuned = _lib.Tuning_t()
+    check(lib.gs3d_get_tuning(ctx, C.byref(tuned)))
+
+    def step(single):
+        for arr in arrs:
+            if single:
+                for i in range(len(arr)):
+                    at = C.c_void_p(C.addressof(arr) + i * C.sizeof(_lib.View_t))
+                    check(lib.gs3d_rebin_batch(ctx, at, 1))
+            else:
+                check(lib.gs3d_rebin_batch(ctx, C.cast(arr, C.c_void_p), len(arr)))
+
+    def settle(single):  # size the key buffers for this path
+        for _ in range(3):
+            step(single)
+            rc = lib.gs3d_synchronize(ctx)
+            if rc != _lib.ERR_CAPACITY:
+                check(rc)
+                return
+
+    def timed(single, schedule, graph):
+        check(lib.gs3d_set_schedule(ctx, schedule))
+        check(lib.gs3d_set_flags(ctx, _lib.FLAG_CUDA_GRAPH if graph else 0))
+        settle(single)
+        for _ in range(warmup):
+            step(single)
+        check(lib.gs3d_synchronize(ctx))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            step(single)
+        e1.record(stream)
+        check(lib.gs3d_synchronize(ctx))
+        torch.cuda.synchronize()
+        views_s = steps * n_views / (e0.elapsed_time(e1) * 1e-3)
+        # one eager step with stage events: per-view stage times
+        check(lib.gs3d_set_flags(ctx, _lib.FLAG_STAGE_TIMING))
+        check(lib.gs3d_read_stage_times(ctx, None, None))
+        step(single)
+        check(lib.gs3d_synchronize(ctx))
+        ms = (C.c_double * 7)()
+        cnt = (C.c_uint32 * 7)()
+        check(lib.gs3d_read_stage_times(ctx, ms, cnt))
+        st = _lib.ScheduleStatus_t()
+        check(lib.gs3d_get_schedule_status(ctx, C.byref(st)))
+        check(lib.gs3d_set_flags(ctx, 0))
+        return {"views_per_s": round(views_s, 2),
+                "stage_ms_per_view": {nm: round(ms[i] / n_views, 4)
+                                      for i, nm in enumerate(_lib.STAGE_NAMES) if cnt[i]},
+                "split_tiles_last_rebin": st.split_tiles,
+                "gate": {"active": ["row_major", "key_count", "learned"][st.active],
+                         "mae_log": round(st.mae_log, 4), "bound": st.bound,
+                         "frames": st.frames, "fallbacks": st.fallbacks}
+                if schedule == _lib.SCHEDULE_LEARNED else None}
+
+    res = {"views": n_views, "batches": [len(a) for a in arrs],
+           "tuning": {"tile": tuned.tile_w, "digit_bits": tuned.digit_bits,
+                      "raster_batch": tuned.raster_batch}}
+    learned_sched, model = install_cost_model(lib, ctx, tuned.tile_w)
+    res["cost_model_checkpoint"] = "trained on the 3M-splat 1080p workload" if model else None
+    # CUDA-graph replay where every batch has one layout (a graph is captured
+    # per layout; alternating layouts would re-capture every call)
+    graph = len(arrs) == 1
+    res["batched_path"] = "CUDA-graph replay" if graph else "eager launches"
+    for label, sc in (("batched_row_major", _lib.SCHEDULE_ROW_MAJOR),
+                      ("batched_key_count", _lib.SCHEDULE_KEY_COUNT),
+                      ("batched_learned", learned_sched)):
+        if label == "batched_learned" and sc != _lib.SCHEDULE_LEARNED:
+            res[label] = None
+            continue
+        res[label] = timed(False, sc, graph)
+    check(lib.gs3d_set_tuning(ctx, C.byref(_lib.Tuning_t(16, 16, 8, 0))))
+    res["single_view_fused_16x16_row_major"] = timed(True, _lib.SCHEDULE_ROW_MAJOR, False)
+    lib.gs3d_destroy(ctx)
+    del stream
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_extras(args):
+    """The batched and skewed-stress configurations beside the headline."""
+    scs, batches = c2_workload()
+    c2 = run_extra_config("batched (4 scenes, 32 mixed views)", scs, batches, None,
+                          args.extra_steps, 1)
+    del scs
+    scs, batches = c4_workload()
+    c4 = run_extra_config("skewed stress (10M, 16 4K views)", scs, batches, (32, 32, 8, 512),
+                          args.extra_steps, 1)
+    return {"batched_4_scenes_32_mixed_views": c2, "skewed_10M_16_views_4k": c4}
 
 
 def profile_run(args):
@@ -609,6 +794,10 @@ def main():
     ap.add_argument("--batch", type=int, default=8, help="views per batched rebin")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched and skewed-stress configurations")
+    ap.add_argument("--extra-steps", type=int, default=3,
+                    help="timed steps of each extra configuration path")
     ap.add_argument("--profile", type=int, default=0, metavar="STEPS",
                     help="profiling run: render STEPS batched steps of --views views and exit "
                          "(no timing, no JSON)")
@@ -645,6 +834,9 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl")
     res = run_ours(args, rank, world)
+    extras = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        extras = run_extras(args)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         times, threads = cpu_view_seconds(1)
@@ -684,8 +876,10 @@ def main():
                        "mean_refs_per_view_16x16": res["mean_refs"],
                        "tile_digit_passes": res["tile_passes_batched"],
                        "single_view_fused_views_per_s": res["fused_value"],
-                       "raster_schedule": "learned (cost MLP)" if res["learned_active"]
-                                          else "key count (cost MLP gated off)",
+                       "raster_schedule": res["best_order"] + " (the fastest of the orders "
+                                          "measured below; every order renders the same "
+                                          "image)",
+                       "cost_model_installed": res["learned_active"],
                        "schedules_single_view": res["schedules"],
                        "schedules_batched_tuned": res["schedules_batched"],
                        "cost_model_heldout": res["cost_model"],
@@ -710,6 +904,7 @@ def main():
                     "rebin_stream_events_value": res["e2e_stream_value"]},
             "gpu_launches": res["launches_per_step"] * args.steps,
             "clocks": res["clocks"],
+            "configs_extra": extras,
         }
         print(json.dumps(out))
     if world > 1:
