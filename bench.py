@@ -751,7 +751,11 @@ def profile_run(args):
     tile, digit_bits, raster_batch = (int(x) for x in args.tuning.split(","))
     assert lib.gs3d_set_tuning(ctx, C.byref(_lib.Tuning_t(tile, tile, digit_bits,
                                                            raster_batch))) == 0
-    schedule, _ = install_cost_model(lib, ctx, tile)
+    if args.order == "learned":
+        schedule, _ = install_cost_model(lib, ctx, tile)
+    else:
+        schedule = {"row_major": _lib.SCHEDULE_ROW_MAJOR,
+                    "key_count": _lib.SCHEDULE_KEY_COUNT}[args.order]
     assert lib.gs3d_set_schedule(ctx, schedule) == 0
     B = args.batch
     for step in range(args.profile):
@@ -803,6 +807,8 @@ def main():
                          "(no timing, no JSON)")
     ap.add_argument("--tuning", default=f"{TILE},8,0", metavar="TILE,DIGIT_BITS,RASTER_BATCH",
                     help="profiling run: the tuning to render with (the bench autotunes)")
+    ap.add_argument("--order", default="key_count", choices=["row_major", "key_count", "learned"],
+                    help="profiling run: the raster order")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
