@@ -128,18 +128,25 @@ __device__ __forceinline__ float splat_alpha(float pfx, float pfy, const SplatSt
   const float4 a = s.a, b = s.b;
   const float dx = pfx - a.x;
   const float dy = pfy - a.y;
-  float d2, q, ev;
   if (s.c.w == 0.0f) {
-    d2 = fmaf(dx, dx, dy * dy);
-    q = fmaf(b.x * dx, dx, fmaf(b.y * dx, dy, b.z * dy * dy));  // = -power * log2(e)
-    ev = -q;
-  } else {  // the reference's order: d^2 = dx dx + dy dy, s = (c0 dx) dx + (2 c1 dx) dy + (c2 dy) dy
-    d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-    q = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(b.x, dx), dx), __fmul_rn(__fmul_rn(b.y, dx), dy)),
-                  __fmul_rn(__fmul_rn(b.z, dy), dy));
-    ev = __fmul_rn(q, -kHalfLog2e);  // exp(-s/2) = 2^(-s log2(e)/2)
+    // fast form: q < 0 cannot occur (no power > 0 test needed): these splats'
+    // conics have condition numbers below 455 (their terms, at least 9 times
+    // the condition number, stay within kExactFormBound), so q, computed to
+    // a relative 1e-3, and the reference's s keep the sign of the positive
+    // definite form at every pixel centre, which lies 6e-8 pixels or more
+    // from the mean unless exactly on it
+    const float d2 = fmaf(dx, dx, dy * dy);
+    const float q = fmaf(b.x * dx, dx, fmaf(b.y * dx, dy, b.z * dy * dy));  // -power log2(e)
+    const float alpha = fminf(0.99f, a.w * ex2_approx(-q));
+    ok = !(d2 > a.z) && !(alpha < 1.0f / 255.0f);
+    return alpha;
   }
-  const float alpha = fminf(0.99f, a.w * ex2_approx(ev));
+  // the reference's order: d^2 = dx dx + dy dy, s = (c0 dx) dx + (2 c1 dx) dy + (c2 dy) dy
+  const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
+  const float q = __fadd_rn(
+      __fadd_rn(__fmul_rn(__fmul_rn(b.x, dx), dx), __fmul_rn(__fmul_rn(b.y, dx), dy)),
+      __fmul_rn(__fmul_rn(b.z, dy), dy));
+  const float alpha = fminf(0.99f, a.w * ex2_approx(__fmul_rn(q, -kHalfLog2e)));  // exp(-s/2)
   ok = !(d2 > a.z) && !(q < 0.0f) && !(alpha < 1.0f / 255.0f);
   return alpha;
 }
@@ -187,11 +194,16 @@ __device__ __forceinline__ float2 splat_alpha2(float pfx, float2 pfy, const Spla
   const float dx = pfx - a.x;
   const float2 dy = __fadd2_rn(pfy, bcast(-a.y));
   float2 d2, q, ev;
-  if (s.c.w == 0.0f) {  // fast form (splat-uniform branch)
+  if (s.c.w == 0.0f) {  // fast form (splat-uniform branch; no q < 0 test, see splat_alpha)
     d2 = __ffma2_rn(bcast(dx), bcast(dx), __fmul2_rn(dy, dy));
     q = __ffma2_rn(bcast(b.x * dx), bcast(dx),
                    __ffma2_rn(bcast(b.y * dx), dy, __fmul2_rn(__fmul2_rn(bcast(b.z), dy), dy)));
-    ev = make_float2(-q.x, -q.y);
+    const float2 e = make_float2(ex2_approx(-q.x), ex2_approx(-q.y));
+    const float2 am = __fmul2_rn(bcast(a.w), e);
+    const float2 alpha = make_float2(fminf(0.99f, am.x), fminf(0.99f, am.y));
+    ok0 = !(d2.x > a.z) && !(alpha.x < 1.0f / 255.0f);
+    ok1 = !(d2.y > a.z) && !(alpha.y < 1.0f / 255.0f);
+    return alpha;
   } else {  // exact form in the reference's order, the column's dx terms shared; the
             // products are paired, every sum a scalar __fadd_rn (never merged into an FMA)
     const float dxx = __fmul_rn(dx, dx);
