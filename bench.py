@@ -203,7 +203,7 @@ def algorithmic_bytes(n, R, tiles, tile_passes, sh_floats, fused, views_per_scen
 # units it processes: tile-digit pass per ref (32x32 / 16x16 tiles);
 # preprocess per scene splat read + per splat-view written; emit per
 # (splat-view, ref) at 32x32 tiles with one-word rectangles.
-DRAM_PER_REF_PASS = {32: 22.6, 16: 25.1}
+DRAM_PER_REF_PASS = {32: 22.4, 16: 25.1}
 DRAM_PREPROCESS = (732.1e6 / 3e6, 434.7e6 / 6e6)
 DRAM_EMIT = {32: (365.2e6, 6e6, 23.7e6)}
 
@@ -222,10 +222,11 @@ def dominant_traffic(stage, tile, refs_per_launch, splats_per_launch, scene_spla
 
 
 # Pipe use of the raster kernel (ncu --set full, one launch of the headline
-# path's raster at 32x32 tiles; profiles/raster_culled_3M_sh3_1080p.md).
-RASTER_NCU = {"kernel": "raster_kernel_culled2", "issue_active": 0.728, "pipe_fma": 0.466,
-              "pipe_alu": 0.608, "warps_active": 0.496,
-              "source": "profiles/raster_culled_3M_sh3_1080p.md"}
+# path's raster at 32x32 tiles, 2-view batch;
+# profiles/raster_culled2_t32_2views_3M_sh3_1080p.md).
+RASTER_NCU = {"kernel": "raster_kernel_culled2", "issue_active": 0.739, "pipe_fma": 0.443,
+              "pipe_alu": 0.602, "pipe_xu": 0.169, "warps_active": 0.496,
+              "source": "profiles/raster_culled2_t32_2views_3M_sh3_1080p.md"}
 
 
 def raster_work(view=0, tile=TILE):
