@@ -79,6 +79,75 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Adds the refs of one rectangle row, global tile ids [a, a + w), to the
+// histogram of one tile-id digit place ((id >> shift) & mask).  The first
+// place (shift 0) is kept as a circular difference array: w ids starting at
+// bin a & mask cover the bins (w >> bits) times over, then the circular run
+// [a & mask, + w % bins), i.e. +1 at its start, -1 past its end, and +1 at
+// bin 0 when it wraps; its counts are the inclusive prefix sums
+// (hist_from_diff_kernel).  Higher places see a row as runs of 2^shift ids
+// per digit value, a few at most.
+__device__ __forceinline__ void row_histogram(uint32_t* hist, uint32_t a, uint32_t w, int shift,
+                                              uint32_t mask) {
+  if (shift == 0) {
+    const uint32_t bins = mask + 1u;
+    const uint32_t full = w / bins, rem = w % bins;
+    if (full) atomicAdd(hist, full);
+    if (rem) {
+      const uint32_t a0 = a & mask, e = a0 + rem;
+      atomicAdd(hist + a0, 1u);
+      if (e < bins) {
+        atomicAdd(hist + e, 0xffffffffu);
+      } else if (e > bins) {
+        atomicAdd(hist + (e - bins), 0xffffffffu);
+        atomicAdd(hist, 1u);
+      }
+    }
+    return;
+  }
+  const uint64_t end = (uint64_t)a + w;
+  for (uint64_t cur = a; cur < end;) {
+    const uint64_t v = cur >> shift;
+    const uint64_t next = min(end, (v + 1) << shift);
+    atomicAdd(hist + (v & mask), (uint32_t)(next - cur));
+    cur = next;
+  }
+}
+
+// Counts of the first tile-digit place from its difference array (one
+// block): inclusive prefix sum of bins <= 2048 entries in place.
+constexpr int kDiffThreads = 256;
+__global__ void __launch_bounds__(kDiffThreads) hist_from_diff_kernel(uint32_t* __restrict__ h,
+                                                                      uint32_t bins) {
+  __shared__ uint32_t s_warp[kDiffThreads / 32];
+  const uint32_t per = (bins + kDiffThreads - 1) / kDiffThreads;  // <= 8
+  const uint32_t b0 = threadIdx.x * per;
+  uint32_t v[8];
+  uint32_t sum = 0;
+#pragma unroll
+  for (uint32_t k = 0; k < 8; ++k) {
+    v[k] = (k < per && b0 + k < bins) ? h[b0 + k] : 0u;
+    sum += v[k];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t inc = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += y;
+  }
+  if (lane == 31) s_warp[warp] = inc;
+  __syncthreads();
+  uint32_t base = 0;
+  for (int w = 0; w < warp; ++w) base += s_warp[w];
+  uint32_t run = base + inc - sum;
+#pragma unroll
+  for (uint32_t k = 0; k < 8; ++k) {
+    run += v[k];
+    if (k < per && b0 + k < bins) h[b0 + k] = run;
+  }
+}
+
 // Fused-rebin emit over a batch: block b owns depth-sorted positions
 // [256b, 256b+256); the splat-view at position i is g = sorted_ids[i], it
 // belongs to the view v whose range holds g, and its refs start at
@@ -156,6 +225,18 @@ __global__ void __launch_bounds__(kThreads)
   }
   const int sh[4] = {shifts.x, shifts.y, shifts.z, shifts.w};
   const uint32_t mk[4] = {masks.x, masks.y, masks.z, masks.w};
+  // the histograms of the tile-digit places the passes sort, a splat row at
+  // a time: each row of a splat's rectangle is a run of consecutive global
+  // tile ids (culled splats have no refs)
+  if (TP > 0 && threadIdx.x < nloc && s_off[threadIdx.x + 1] != s_off[threadIdx.x]) {
+    const uint4 ra = s_ra[threadIdx.x];
+    const uint32_t w = ra.y, h = ra.x / ra.y, stride = ra.w + ra.y;  // stride = tiles_x
+    const uint32_t first_tile = s_rb[threadIdx.x].x;
+    for (uint32_t r = 0; r < h; ++r) {
+#pragma unroll
+      for (int p = 0; p < TP; ++p) row_histogram(s_hist[p], first_tile + r * stride, w, sh[p], mk[p]);
+    }
+  }
   // Each warp expands a contiguous share of the block's refs, 32 at a time.
   // The owner of a ref is the last splat starting at or before it.  The
   // owners of a 32-ref chunk are the owner c0 of its first ref and the
@@ -196,9 +277,7 @@ __global__ void __launch_bounds__(kThreads)
       o = lo;
     }
     c0 = __shfl_sync(0xffffffffu, o, 31);  // owner of the chunk's last ref
-    bool live = j < wend;
-    uint32_t tile = 0;
-    if (live) {
+    if (j < wend) {
       const uint32_t k = j - s_off[o];
       const uint4 ra = s_ra[o];
       if (k < ra.x) {
@@ -206,15 +285,10 @@ __global__ void __launch_bounds__(kThreads)
         // (k < w * h <= tiles of one view)
         const uint32_t row = (uint32_t)(((float)k + 0.5f) * __uint_as_float(ra.z));
         const uint4 rb = s_rb[o];
-        tile = rb.x + row * ra.w + k;
-        keys[j] = make_uint2(tile, rb.y);
+        keys[j] = make_uint2(rb.x + row * ra.w + k, rb.y);
         values[j] = rb.z;
-      } else {
-        live = false;
       }
     }
-#pragma unroll
-    for (int p = 0; p < TP; ++p) hist_add_256(s_hist[p], (tile >> sh[p]) & mk[p], live);
   }
   __syncthreads();
   for (int k = threadIdx.x; k < TP * BINS; k += kThreads) {
@@ -272,6 +346,10 @@ cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t
     }
   }
 #undef GS3D_EMIT_CASE
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || tile_plan.passes == 0) return e;
+  // the first (shift 0) place was accumulated as a difference array
+  hist_from_diff_kernel<<<1, kDiffThreads, 0, s>>>(g_hist, digit_mask(tile_plan.nbits[0]) + 1u);
   return cudaGetLastError();
 }
 
