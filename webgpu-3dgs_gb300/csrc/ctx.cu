@@ -625,7 +625,8 @@ int fused_rebin(gs3d_ctx* c) {
                           u32(c->depth_ids_a),
                           u32(c->sorted_offsets), u32(c->ref_counter), c->capacity,
                           static_cast<uint2*>(c->keys_a.p), u32(c->vals_a), tp,
-                          &k->tile_hist[0][0], &k->error, c->stream),
+                          &k->tile_hist[0][0], &k->emit_chunk, &k->error, c->sm_count,
+                          c->stream),
        "emit (depth order)");
   }
   {

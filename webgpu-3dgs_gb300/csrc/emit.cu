@@ -14,6 +14,8 @@
 // access (emit_tile_refs.wgsl:68-77).  Here the live count is compared with
 // the key capacity first; on overflow nothing is written and
 // DEVERR_CAPACITY is latched.
+#include <algorithm>
+
 #include "gs3d_internal.cuh"
 
 namespace gs3d {
@@ -79,83 +81,23 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// Adds the refs of one rectangle row, global tile ids [a, a + w), to the
-// histogram of one tile-id digit place ((id >> shift) & mask).  The first
-// place (shift 0) is kept as a circular difference array: w ids starting at
-// bin a & mask cover the bins (w >> bits) times over, then the circular run
-// [a & mask, + w % bins), i.e. +1 at its start, -1 past its end, and +1 at
-// bin 0 when it wraps; its counts are the inclusive prefix sums
-// (hist_from_diff_kernel).  Higher places see a row as runs of 2^shift ids
-// per digit value, a few at most.
-__device__ __forceinline__ void row_histogram(uint32_t* hist, uint32_t a, uint32_t w, int shift,
-                                              uint32_t mask) {
-  if (shift == 0) {
-    const uint32_t bins = mask + 1u;
-    const uint32_t full = w / bins, rem = w % bins;
-    if (full) atomicAdd(hist, full);
-    if (rem) {
-      const uint32_t a0 = a & mask, e = a0 + rem;
-      atomicAdd(hist + a0, 1u);
-      if (e < bins) {
-        atomicAdd(hist + e, 0xffffffffu);
-      } else if (e > bins) {
-        atomicAdd(hist + (e - bins), 0xffffffffu);
-        atomicAdd(hist, 1u);
-      }
-    }
-    return;
-  }
-  const uint64_t end = (uint64_t)a + w;
-  for (uint64_t cur = a; cur < end;) {
-    const uint64_t v = cur >> shift;
-    const uint64_t next = min(end, (v + 1) << shift);
-    atomicAdd(hist + (v & mask), (uint32_t)(next - cur));
-    cur = next;
-  }
-}
-
-// Counts of the first tile-digit place from its difference array (one
-// block): inclusive prefix sum of bins <= 2048 entries in place.
-constexpr int kDiffThreads = 256;
-__global__ void __launch_bounds__(kDiffThreads) hist_from_diff_kernel(uint32_t* __restrict__ h,
-                                                                      uint32_t bins) {
-  __shared__ uint32_t s_warp[kDiffThreads / 32];
-  const uint32_t per = (bins + kDiffThreads - 1) / kDiffThreads;  // <= 8
-  const uint32_t b0 = threadIdx.x * per;
-  uint32_t v[8];
-  uint32_t sum = 0;
-#pragma unroll
-  for (uint32_t k = 0; k < 8; ++k) {
-    v[k] = (k < per && b0 + k < bins) ? h[b0 + k] : 0u;
-    sum += v[k];
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t inc = sum;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += y;
-  }
-  if (lane == 31) s_warp[warp] = inc;
-  __syncthreads();
-  uint32_t base = 0;
-  for (int w = 0; w < warp; ++w) base += s_warp[w];
-  uint32_t run = base + inc - sum;
-#pragma unroll
-  for (uint32_t k = 0; k < 8; ++k) {
-    run += v[k];
-    if (k < per && b0 + k < bins) h[b0 + k] = run;
-  }
-}
-
-// Fused-rebin emit over a batch: block b owns depth-sorted positions
-// [256b, 256b+256); the splat-view at position i is g = sorted_ids[i], it
+// Fused-rebin emit over a batch: chunk c holds the depth-sorted positions
+// [256c, 256c+256); the splat-view at position i is g = sorted_ids[i], it
 // belongs to the view v whose range holds g, and its refs start at
 // sorted_offsets[i].  Keys carry global tile ids (view tile base + local
 // tile) so the later tile-digit passes also separate the views; values carry
 // g.  Besides the keys/values the kernel accumulates the 256-bin histograms
 // of the tile-id digit places those passes sort, so they need no separate
 // histogram read.
+//
+// The grid is the resident blocks of every SM and each block takes chunks
+// from a ticket counter until none are left, keeping its histograms in
+// shared memory across its chunks: the global histogram then takes one atomic
+// per (block, nonzero bin) rather than one per (chunk, nonzero bin).  All
+// blocks add to the same few hundred words, so per-chunk flushes (tens of
+// millions of atomics per batch on a few L2 slices) cost more than the emit's
+// own stores.  Tickets rather than a fixed stride, because the refs of a chunk
+// range from 256 to millions (near splats covering a whole view).
 template <int TP, int BINS>
 __global__ void __launch_bounds__(kThreads)
     emit_sorted_kernel(const ViewDesc* __restrict__ views, uint32_t n_views, uint32_t n,
@@ -166,13 +108,15 @@ __global__ void __launch_bounds__(kThreads)
                        const uint32_t* __restrict__ sorted_offsets,
                        const uint32_t* __restrict__ ref_counter, uint32_t capacity,
                        uint2* __restrict__ keys, uint32_t* __restrict__ values, int4 shifts,
-                       uint4 masks, uint32_t* __restrict__ g_hist, uint32_t* __restrict__ err) {
+                       uint4 masks, uint32_t* __restrict__ g_hist,
+                       uint32_t* __restrict__ chunk_ticket, uint32_t* __restrict__ err) {
   __shared__ uint32_t s_off[kThreads + 1];
   // per splat, read as two 16-byte words by every ref it owns:
   // [count, rectangle width, bits(1/width), tiles_x - width] and
   // [global tile of the rectangle's first tile, depth bits, splat-view id, -]
   __shared__ uint4 s_ra[kThreads], s_rb[kThreads];
   __shared__ uint32_t s_hist[TP > 0 ? TP : 1][BINS];
+  __shared__ uint32_t s_chunk;
 
   const uint32_t total = *ref_counter;
   if (total > capacity) {
@@ -180,114 +124,117 @@ __global__ void __launch_bounds__(kThreads)
     return;
   }
   for (int k = threadIdx.x; k < TP * BINS; k += kThreads) (&s_hist[0][0])[k] = 0u;
-  const uint32_t first = blockIdx.x * kThreads;
-  const uint32_t i = first + threadIdx.x;
-  if (i < n) {
-    // only the tile rectangle is gathered (one 32-byte sector of the record):
-    // the depth bits come in order from the depth sort, the ref count from
-    // the scan's offsets (0 for culled splats, whose rectangle is zeroed)
-    // (or, where every view's tile grid fits 8 bits, the 4-byte word of the
-    // preprocess's compact rectangle array, which stays in L2)
-    const uint32_t id = __ldg(sorted_ids + i);
-    uint32_t x0, y0, w, h;
-    if (rect8 != nullptr) {
-      const uint32_t rr = __ldg(rect8 + id);
-      x0 = rr & 0xffu;
-      y0 = (rr >> 8) & 0xffu;
-      w = ((rr >> 16) & 0xffu) + 1u;
-      h = (rr >> 24) + 1u;
-    } else {
-      const uint4 r3 = __ldg(reinterpret_cast<const uint4*>(proj + id) + 3);
-      x0 = r3.x;
-      y0 = r3.y;
-      w = r3.z - r3.x + 1u;
-      h = r3.w - r3.y + 1u;
-    }
-    const uint32_t v =
-        find_view(n_views, id, [&](uint32_t k) { return __ldg(&views[k].splat_base); });
-    s_off[threadIdx.x] = __ldg(sorted_offsets + i);
-    const uint32_t tx = __ldg(&views[v].f.tile_count[0]);
-    // ref k of the splat: row = k / w, tile = first + row * tx + (k - row * w)
-    //                                      = first + row * (tx - w) + k
-    s_ra[threadIdx.x] = make_uint4(w * h, w, __float_as_uint(1.0f / (float)w), tx - w);
-    s_rb[threadIdx.x] = make_uint4(__ldg(&views[v].f.tile_base) + y0 * tx + x0,
-                                   __ldg(sorted_keys + i), id, 0u);
-  }
-  const uint32_t last = min(n, first + kThreads);
-  if (threadIdx.x == 0) s_off[last - first] = __ldg(sorted_offsets + last);
-  __syncthreads();
-
-  const uint32_t nloc = last - first;
-  const uint32_t begin = s_off[0], end = s_off[nloc];
-  if (end < begin || end > total) {
-    if (threadIdx.x == 0) latch_error(err, DEVERR_RANGE);
-    return;
-  }
   const int sh[4] = {shifts.x, shifts.y, shifts.z, shifts.w};
   const uint32_t mk[4] = {masks.x, masks.y, masks.z, masks.w};
-  // the histograms of the tile-digit places the passes sort, a splat row at
-  // a time: each row of a splat's rectangle is a run of consecutive global
-  // tile ids (culled splats have no refs)
-  if (TP > 0 && threadIdx.x < nloc && s_off[threadIdx.x + 1] != s_off[threadIdx.x]) {
-    const uint4 ra = s_ra[threadIdx.x];
-    const uint32_t w = ra.y, h = ra.x / ra.y, stride = ra.w + ra.y;  // stride = tiles_x
-    const uint32_t first_tile = s_rb[threadIdx.x].x;
-    for (uint32_t r = 0; r < h; ++r) {
-#pragma unroll
-      for (int p = 0; p < TP; ++p) row_histogram(s_hist[p], first_tile + r * stride, w, sh[p], mk[p]);
-    }
-  }
-  // Each warp expands a contiguous share of the block's refs, 32 at a time.
-  // The owner of a ref is the last splat starting at or before it.  The
-  // owners of a 32-ref chunk are the owner c0 of its first ref and the
-  // splats c0+1 .. c0+32 starting inside it; while those starts are
-  // distinct (every valid splat has a ref, and culled splats, which have
-  // none, sort after all valid ones) one OR-reduction of their start bits
-  // gives every lane its owner.  A chunk with equal starts (zero-count
-  // splats) searches per ref instead.
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t share = ((end - begin + kThreads - 1) / kThreads) * 32u;
-  const uint32_t wbeg = min(end, begin + warp * share), wend = min(end, wbeg + share);
-  uint32_t c0 = 0;  // owner of ref wbeg: the last splat starting at or before it
-  {
-    uint32_t lo = 0, hi = nloc;  // invariant: s_off[lo] <= wbeg < s_off[hi]
-    while (hi - lo > 1) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (s_off[mid] <= wbeg) lo = mid; else hi = mid;
+  const uint32_t chunks = (n + kThreads - 1) / kThreads;
+  for (;;) {
+    if (threadIdx.x == 0) s_chunk = atomicAdd(chunk_ticket, 1u);
+    // also: the previous chunk's readers are done with s_off / s_ra / s_rb
+    __syncthreads();
+    const uint32_t chunk = s_chunk;
+    if (chunk >= chunks) break;
+    const uint32_t first = chunk * kThreads;
+    const uint32_t i = first + threadIdx.x;
+    if (i < n) {
+      // only the tile rectangle is gathered (one 32-byte sector of the record):
+      // the depth bits come in order from the depth sort, the ref count from
+      // the scan's offsets (0 for culled splats, whose rectangle is zeroed)
+      // (or, where every view's tile grid fits 8 bits, the 4-byte word of the
+      // preprocess's compact rectangle array, which stays in L2)
+      const uint32_t id = __ldg(sorted_ids + i);
+      uint32_t x0, y0, w, h;
+      if (rect8 != nullptr) {
+        const uint32_t rr = __ldg(rect8 + id);
+        x0 = rr & 0xffu;
+        y0 = (rr >> 8) & 0xffu;
+        w = ((rr >> 16) & 0xffu) + 1u;
+        h = (rr >> 24) + 1u;
+      } else {
+        const uint4 r3 = __ldg(reinterpret_cast<const uint4*>(proj + id) + 3);
+        x0 = r3.x;
+        y0 = r3.y;
+        w = r3.z - r3.x + 1u;
+        h = r3.w - r3.y + 1u;
+      }
+      const uint32_t v =
+          find_view(n_views, id, [&](uint32_t k) { return __ldg(&views[k].splat_base); });
+      s_off[threadIdx.x] = __ldg(sorted_offsets + i);
+      const uint32_t tx = __ldg(&views[v].f.tile_count[0]);
+      // ref k of the splat: row = k / w, tile = first + row * tx + (k - row * w)
+      //                                      = first + row * (tx - w) + k
+      s_ra[threadIdx.x] = make_uint4(w * h, w, __float_as_uint(1.0f / (float)w), tx - w);
+      s_rb[threadIdx.x] = make_uint4(__ldg(&views[v].f.tile_base) + y0 * tx + x0,
+                                     __ldg(sorted_keys + i), id, 0u);
     }
-    c0 = lo;
-  }
-  for (uint32_t cb = wbeg; cb < wend; cb += 32) {  // warp-uniform trip count
-    const uint32_t j = cb + lane;
-    const uint32_t cand = c0 + 1 + lane;
-    const uint32_t st = cand <= nloc ? s_off[cand] : 0xffffffffu;
-    const uint32_t rel = st - cb;
-    const uint32_t down = __shfl_down_sync(0xffffffffu, st, 1);
-    const uint32_t next_st = lane < 31 ? down : (cand < nloc ? s_off[cand + 1] : 0xffffffffu);
-    uint32_t o;
-    if (!__any_sync(0xffffffffu, rel < 32 && next_st == st)) {
-      const uint32_t starts = __reduce_or_sync(0xffffffffu, rel < 32 ? 1u << rel : 0u);
-      o = c0 + __popc(starts & (0xffffffffu >> (31 - lane)));
-    } else {
-      uint32_t lo = c0, hi = nloc;  // s_off[c0] <= cb <= j
+    const uint32_t last = min(n, first + kThreads);
+    if (threadIdx.x == 0) s_off[last - first] = __ldg(sorted_offsets + last);
+    __syncthreads();
+
+    const uint32_t nloc = last - first;
+    const uint32_t begin = s_off[0], end = s_off[nloc];
+    if (end < begin || end > total) {  // block-uniform (shared values): skip the chunk
+      if (threadIdx.x == 0) latch_error(err, DEVERR_RANGE);
+      continue;
+    }
+    // Each warp expands a contiguous share of the block's refs, 32 at a time.
+    // The owner of a ref is the last splat starting at or before it.  The
+    // owners of a 32-ref chunk are the owner c0 of its first ref and the
+    // splats c0+1 .. c0+32 starting inside it; while those starts are
+    // distinct (every valid splat has a ref, and culled splats, which have
+    // none, sort after all valid ones) one OR-reduction of their start bits
+    // gives every lane its owner.  A chunk with equal starts (zero-count
+    // splats) searches per ref instead.
+    const uint32_t share = ((end - begin + kThreads - 1) / kThreads) * 32u;
+    const uint32_t wbeg = min(end, begin + warp * share), wend = min(end, wbeg + share);
+    uint32_t c0 = 0;  // owner of ref wbeg: the last splat starting at or before it
+    {
+      uint32_t lo = 0, hi = nloc;  // invariant: s_off[lo] <= wbeg < s_off[hi]
       while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (s_off[mid] <= j) lo = mid; else hi = mid;
+        if (s_off[mid] <= wbeg) lo = mid; else hi = mid;
       }
-      o = lo;
+      c0 = lo;
     }
-    c0 = __shfl_sync(0xffffffffu, o, 31);  // owner of the chunk's last ref
-    if (j < wend) {
-      const uint32_t k = j - s_off[o];
-      const uint4 ra = s_ra[o];
-      if (k < ra.x) {
-        // row = floor(k / w) by a float reciprocal: exact while k + w < 2^22
-        // (k < w * h <= tiles of one view)
-        const uint32_t row = (uint32_t)(((float)k + 0.5f) * __uint_as_float(ra.z));
-        const uint4 rb = s_rb[o];
-        keys[j] = make_uint2(rb.x + row * ra.w + k, rb.y);
-        values[j] = rb.z;
+    for (uint32_t cb = wbeg; cb < wend; cb += 32) {  // warp-uniform trip count
+      const uint32_t j = cb + lane;
+      const uint32_t cand = c0 + 1 + lane;
+      const uint32_t st = cand <= nloc ? s_off[cand] : 0xffffffffu;
+      const uint32_t rel = st - cb;
+      const uint32_t down = __shfl_down_sync(0xffffffffu, st, 1);
+      const uint32_t next_st = lane < 31 ? down : (cand < nloc ? s_off[cand + 1] : 0xffffffffu);
+      uint32_t o;
+      if (!__any_sync(0xffffffffu, rel < 32 && next_st == st)) {
+        const uint32_t starts = __reduce_or_sync(0xffffffffu, rel < 32 ? 1u << rel : 0u);
+        o = c0 + __popc(starts & (0xffffffffu >> (31 - lane)));
+      } else {
+        uint32_t lo = c0, hi = nloc;  // s_off[c0] <= cb <= j
+        while (hi - lo > 1) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (s_off[mid] <= j) lo = mid; else hi = mid;
+        }
+        o = lo;
       }
+      c0 = __shfl_sync(0xffffffffu, o, 31);  // owner of the chunk's last ref
+      bool live = j < wend;
+      uint32_t tile = 0;
+      if (live) {
+        const uint32_t k = j - s_off[o];
+        const uint4 ra = s_ra[o];
+        if (k < ra.x) {
+          // row = floor(k / w) by a float reciprocal: exact while k + w < 2^22
+          // (k < w * h <= tiles of one view)
+          const uint32_t row = (uint32_t)(((float)k + 0.5f) * __uint_as_float(ra.z));
+          const uint4 rb = s_rb[o];
+          tile = rb.x + row * ra.w + k;
+          keys[j] = make_uint2(tile, rb.y);
+          values[j] = rb.z;
+        } else {
+          live = false;
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < TP; ++p) hist_add_256(s_hist[p], (tile >> sh[p]) & mk[p], live);
     }
   }
   __syncthreads();
@@ -295,6 +242,23 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t v = (&s_hist[0][0])[k];
     if (v) atomicAdd(g_hist + (k / BINS) * kTileHistStride + k % BINS, v);
   }
+}
+
+// Resident blocks per SM of one emit instance (its registers and shared
+// memory decide), asked once per instance.
+template <int TP, int BINS>
+uint32_t emit_blocks_per_sm() {
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, emit_sorted_kernel<TP, BINS>, kThreads,
+                                                      0) != cudaSuccess) {
+      (void)cudaGetLastError();
+      b = 1;
+    }
+    per_sm = b < 1 ? 1 : b;
+  }
+  return (uint32_t)per_sm;
 }
 
 }  // namespace
@@ -305,10 +269,12 @@ cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t
                                const uint32_t* sorted_ids,
                                const uint32_t* sorted_offsets, const uint32_t* ref_counter,
                                uint32_t capacity, uint2* keys, uint32_t* values,
-                               const SortPlan& tile_plan, uint32_t* g_hist, uint32_t* err,
+                               const SortPlan& tile_plan, uint32_t* g_hist,
+                               uint32_t* chunk_ticket, uint32_t* err, int sm_count,
                                cudaStream_t s) {
   if (n == 0) return cudaSuccess;
-  const uint32_t blocks = (n + kThreads - 1) / kThreads;
+  const uint32_t chunks = (n + kThreads - 1) / kThreads;
+  const uint32_t sms = sm_count > 0 ? (uint32_t)sm_count : 1u;
   int4 sh = make_int4(0, 0, 0, 0);
   uint4 mk = make_uint4(0, 0, 0, 0);
   int* shp = &sh.x;
@@ -321,10 +287,10 @@ cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t
   for (int p = 0; p < tile_plan.passes; ++p) wide = wide || tile_plan.nbits[p] > 8;
 #define GS3D_EMIT_CASE(TP, BINS)                                                              \
   case TP:                                                                                    \
-    emit_sorted_kernel<TP, BINS><<<blocks, kThreads, 0, s>>>(                                 \
+    emit_sorted_kernel<TP, BINS><<<std::min(chunks, sms * emit_blocks_per_sm<TP, BINS>()),    \
+                                   kThreads, 0, s>>>(                                         \
         views, n_views, n, proj, rect8, sorted_keys, sorted_ids, sorted_offsets, ref_counter, \
-        capacity, keys,                                                                       \
-        values, sh, mk, g_hist, err);                                                         \
+        capacity, keys, values, sh, mk, g_hist, chunk_ticket, err);                           \
     break;
   if (wide) {
     switch (tile_plan.passes) {
@@ -346,10 +312,6 @@ cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t
     }
   }
 #undef GS3D_EMIT_CASE
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess || tile_plan.passes == 0) return e;
-  // the first (shift 0) place was accumulated as a difference array
-  hist_from_diff_kernel<<<1, kDiffThreads, 0, s>>>(g_hist, digit_mask(tile_plan.nbits[0]) + 1u);
   return cudaGetLastError();
 }
 

@@ -87,7 +87,8 @@ struct Ctrl {
   uint32_t raster_queue;
   uint32_t sched_counter[2];
   uint32_t raster_heavy;  // tiles at the head of the raster order shaded as half strips
-  uint32_t pad[2];
+  uint32_t emit_chunk;    // next 256-splat chunk of the depth-ordered emit
+  uint32_t pad;
   uint32_t sort_hist[kMaxSortPasses][kRadixBins];  // global digit histograms
   uint32_t sched_hist[2][kRadixBins];
   uint32_t tile_hist[kMaxTilePasses][kTileHistStride];  // fused rebin's tile passes
@@ -362,7 +363,8 @@ cudaError_t launch_emit_sorted(const ViewDesc* views, uint32_t n_views, uint32_t
                                const uint32_t* sorted_ids,
                                const uint32_t* sorted_offsets, const uint32_t* ref_counter,
                                uint32_t capacity, uint2* keys, uint32_t* values,
-                               const SortPlan& tile_plan, uint32_t* g_hist, uint32_t* err,
+                               const SortPlan& tile_plan, uint32_t* g_hist,
+                               uint32_t* chunk_ticket, uint32_t* err, int sm_count,
                                cudaStream_t s);
 cudaError_t launch_identify(const uint2* keys, const uint32_t* ref_counter, uint32_t capacity,
                             uint32_t num_tiles, uint32_t* tile_offsets, uint32_t* err,

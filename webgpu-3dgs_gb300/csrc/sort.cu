@@ -870,10 +870,9 @@ size_t sort_status_words_max(uint32_t capacity) {
 cudaError_t launch_sort(const SortPlan& plan, const uint32_t* ref_counter, uint32_t capacity,
                         uint2* keys_a, uint32_t* vals_a, uint2* keys_b, uint32_t* vals_b,
                         uint32_t* status, Ctrl* ctrl, int sm_count, cudaStream_t s) {
-  cudaError_t e = cudaMemsetAsync(ctrl->sort_part_counter, 0,
-                                  sizeof(ctrl->sort_part_counter) + sizeof(ctrl->pad) +
-                                      sizeof(ctrl->sort_hist),
-                                  s);
+  // the sort may run more than once per frame: its tickets and histograms
+  cudaError_t e = cudaMemsetAsync(ctrl->sort_part_counter, 0, sizeof(ctrl->sort_part_counter), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctrl->sort_hist, 0, sizeof(ctrl->sort_hist), s);
   if (e != cudaSuccess) return e;
   return run_passes<uint2>(plan, ref_counter, capacity, keys_a, vals_a, keys_b, vals_b, status,
                            &ctrl->sort_hist[0][0], kRadixBins, ctrl->sort_part_counter,
