@@ -559,8 +559,6 @@ int raster_stage(gs3d_ctx* c, bool culled) {
   a.tile_costs = u32(c->tile_costs);
   a.order = order;
   a.queue_counter = &ctrl_of(c)->raster_queue;
-  a.batch = c->raster_batch;
-  a.culled = culled;
   CK(cudaMemsetAsync(a.queue_counter, 0, sizeof(uint32_t), c->stream), "reset raster queue");
   // the previous frame's splat target may still be copying out (captured as
   // an external event wait in graph mode; a never-recorded event is no wait)

@@ -37,6 +37,7 @@ namespace gs3d {
 namespace {
 
 constexpr int kThreads = 256;   // histogram kernel
+constexpr int kHistItems = 16;  // keys a histogram thread loads per round
 constexpr int kPassThreads = 512;                  // onesweep pass (8-bit and narrower digits)
 constexpr int kWarps = kPassThreads / 32;          // 16
 constexpr int kItems = 8;
@@ -145,13 +146,24 @@ __global__ void __launch_bounds__(kThreads)
     shift[p] = pd.shift[p];
     mask[p] = pd.mask[p];
   }
-  for (size_t base = (size_t)blockIdx.x * kThreads; base < R; base += gstride) {
-    const size_t idx = base + threadIdx.x;
-    const bool in = idx < R;
-    const K k = in ? keys[idx] : KeyOps<K>::sentinel();
+  // kHistItems keys a thread per round, all loads issued before the first
+  // histogram add: one load in flight per thread would leave the kernel at a
+  // fraction of HBM bandwidth behind its shared-memory atomics
+  const size_t rstride = gstride * kHistItems;
+  for (size_t base = (size_t)blockIdx.x * kThreads * kHistItems; base < R; base += rstride) {
+    K k[kHistItems];
 #pragma unroll
-    for (int p = 0; p < P; ++p)
-      hist_add_256(s_hist[p], KeyOps<K>::digit(k, word[p], shift[p]) & mask[p], in);
+    for (int i = 0; i < kHistItems; ++i) {
+      const size_t idx = base + (size_t)i * kThreads + threadIdx.x;
+      k[i] = idx < R ? keys[idx] : KeyOps<K>::sentinel();
+    }
+#pragma unroll
+    for (int i = 0; i < kHistItems; ++i) {
+      const bool in = base + (size_t)i * kThreads + threadIdx.x < R;
+#pragma unroll
+      for (int p = 0; p < P; ++p)
+        hist_add_256(s_hist[p], KeyOps<K>::digit(k[i], word[p], shift[p]) & mask[p], in);
+    }
   }
   __syncthreads();
   for (int k = threadIdx.x; k < P * kRadixBins; k += kThreads) {
