@@ -437,13 +437,13 @@ int gs3d_read_tile_counts(struct gs3d_ctx* ctx, uint32_t* counts, size_t n);
  *     the current device and returns without waiting;
  *   - n may be at most 67,108,864 (2^26); larger n is rejected with
  *     GS3D_ERR_INVALID_ARG and a message in gs3d_last_error(NULL);
- *   - the first call on each device looks up the scratch array's device
- *     address (set-up), so make it before any stream capture;
+ *   - the first call on each device loads the library's kernels and scratch
+ *     array on it, so make it before any stream capture (later calls only
+ *     look the scratch address up again, which stays valid across a reset
+ *     of the device);
  *   - every call on a device shares the one scratch array: calls whose
  *     kernels overlap on the GPU (different streams, no ordering between
  *     them) race and give wrong offsets; order them on one stream;
- *   - the scratch address is looked up once per device and kept: do not
- *     reset the device (cudaDeviceReset) while the library is loaded;
  *   - GS3D_OK means the scan was enqueued, not that it succeeded: the device
  *     errors it can meet (a total of 2^32 or more, a look-back wait that gave
  *     up) are latched in the scratch array and reported by

@@ -31,8 +31,18 @@ struct NoAllocScratch {
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
 std::mutex g_mutex;
-NoAllocScratch* g_scratch_ptr[gs3d::kMaxDevices] = {};  // device address, per device
-uint32_t g_epoch[gs3d::kMaxDevices] = {};               // look-back epoch, per device
+bool g_ran[gs3d::kMaxDevices] = {};        // a scan has been launched on the device
+uint32_t g_epoch[gs3d::kMaxDevices] = {};  // look-back epoch, per device
+
+// The scratch block's device address on the current device, queried on
+// every call: the query allocates nothing, and a context that was reset may
+// load the module at another address.
+cudaError_t scratch_address(NoAllocScratch** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  *out = static_cast<NoAllocScratch*>(p);
+  return e;
+}
 thread_local char g_error[256] = "no error";
 
 int fail(int code, const char* msg) {
@@ -62,27 +72,21 @@ extern "C" int gs3d_prefix_scan_noalloc(const uint32_t* counts, uint32_t* offset
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= gs3d::kMaxDevices)
     return fail(GS3D_ERR_NO_DEVICE, "gs3d_prefix_scan_noalloc: no current CUDA device");
+  // the host-side symbol is only a stand-in: the kernel needs the device address
   NoAllocScratch* scratch = nullptr;
+  e = scratch_address(&scratch);
+  if (e != cudaSuccess) {
+    snprintf(msg, sizeof(msg), "gs3d_prefix_scan_noalloc: cudaGetSymbolAddress failed: %s",
+             cudaGetErrorString(e));
+    cudaGetLastError();
+    return fail(e == cudaErrorNoKernelImageForDevice ? GS3D_ERR_NO_DEVICE : GS3D_ERR_CUDA, msg);
+  }
   uint32_t epoch = 0;
   {
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (g_scratch_ptr[dev] == nullptr) {
-      // set-up, once per device, with that device current: the host-side
-      // symbol is only a stand-in, the kernel needs the device address
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess) {
-        snprintf(msg, sizeof(msg), "gs3d_prefix_scan_noalloc: cudaGetSymbolAddress failed: %s",
-                 cudaGetErrorString(e));
-        cudaGetLastError();
-        return fail(e == cudaErrorNoKernelImageForDevice ? GS3D_ERR_NO_DEVICE : GS3D_ERR_CUDA,
-                    msg);
-      }
-      g_scratch_ptr[dev] = static_cast<NoAllocScratch*>(p);
-    }
-    scratch = g_scratch_ptr[dev];
     g_epoch[dev] = (g_epoch[dev] % ((1u << 30) - 1)) + 1;  // 1 .. 2^30-1, never 0
     epoch = g_epoch[dev];
+    g_ran[dev] = true;
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // the ticket and the error word must start at zero; the status words are
@@ -108,15 +112,16 @@ extern "C" int gs3d_prefix_scan_noalloc_status(void* stream) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= gs3d::kMaxDevices)
     return fail(GS3D_ERR_NO_DEVICE, "gs3d_prefix_scan_noalloc_status: no current CUDA device");
-  NoAllocScratch* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_mutex);
-    scratch = g_scratch_ptr[dev];
+    if (!g_ran[dev]) return GS3D_OK;  // no scan has run on this device
   }
-  if (scratch == nullptr) return GS3D_OK;  // no scan has run on this device
+  NoAllocScratch* scratch = nullptr;
+  e = scratch_address(&scratch);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   uint32_t word = 0;
-  e = cudaMemcpyAsync(&word, &scratch->error, sizeof(word), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&word, &scratch->error, sizeof(word), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     char msg[200];
