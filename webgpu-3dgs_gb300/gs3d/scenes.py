@@ -137,6 +137,36 @@ def scene_skewed(n: int = 10_000_000, seed: int = 0, sh_degree: int = 3) -> Gaus
     return activate(xyz, f_dc, opacity, scale_log, rot, f_rest, sh_degree)
 
 
+def scene_opacity_mix(n_opaque: int = 1_500_000, n_translucent: int = 400_000,
+                      seed: int = 0) -> GaussianSplatData:
+    """A frame of skewed tile costs, SH degree 0: 12 opaque clusters (centres
+    in a radius-7 ball, sigma ~ U(0.3, 0.9), scale exp(N(-4.2, 0.6^2)),
+    opacity sigmoid(N(4, 0.5^2)): many keys per tile, pixels terminate after
+    a few dozen) beside 6 dense translucent ones (sigma ~ U(0.05, 0.15), scale
+    exp(N(-3, 0.4^2)), opacity sigmoid(N(-5, 0.15^2)), alpha near the 1/255
+    cut-off: no pixel terminates, every key of their tiles is iterated)."""
+    rng = np.random.default_rng(seed + 3000)
+
+    def clusters(n, k, smin, smax):
+        d = rng.standard_normal((k, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        c = d * (7.0 * rng.random(k) ** (1.0 / 3.0))[:, None]
+        sigma = rng.uniform(smin, smax, k)
+        which = rng.integers(0, k, n)
+        return c[which] + sigma[which, None] * rng.standard_normal((n, 3))
+
+    n = n_opaque + n_translucent
+    xyz = np.concatenate([clusters(n_opaque, 12, 0.3, 0.9),
+                          clusters(n_translucent, 6, 0.05, 0.15)]).astype(np.float32)
+    scale_log = np.concatenate([_normal(rng, (n_opaque, 3), -4.2, 0.6),
+                                _normal(rng, (n_translucent, 3), -3.0, 0.4)])
+    opacity = np.concatenate([_normal(rng, n_opaque, 4.0, 0.5),
+                              _normal(rng, n_translucent, -5.0, 0.15)])
+    rot = _normal(rng, (n, 4))
+    f_dc = _normal(rng, (n, 3), 0.0, 0.5)
+    return activate(xyz, f_dc, opacity, scale_log, rot, None, 0)
+
+
 FOVY = math.radians(60.0)
 NEAR = 0.2
 FAR = 10000.0  # the reference's Viewport default far plane (src/Viewport.ts:58-66)
