@@ -597,11 +597,29 @@ def c4_workload():
     return [data], [cv[0:2], cv[2:4], cv[4:6], cv[6:8], wv]
 
 
-def run_extra_config(name, scenes_data, batches, tuning, steps, warmup):
+def tail_workload():
+    """A tail-bound workload: scene_opacity_mix (1.5M opaque splats in 12
+    clusters beside 0.4M translucent ones in 6 dense clusters, SH 0), 1080p,
+    16x16 tiles; the cost model is trained on 120 random poses and 16 held-out
+    poses are rendered, as two batches of 8."""
+    from gs3d import scenes
+    data = scenes.scene_opacity_mix(1_500_000, 400_000, seed=3)
+    W, H = 1920, 1080
+    us = [scenes.camera_at(e, W, H).getUniformData(W, H)
+          for e in scenes.random_eyes(136, 9.0, 16.0, seed=9)]
+    views = [(0, u, W, H) for u in us[120:]]
+    return [data], [views[:8], views[8:]], (us[:120], W, H)
+
+
+def run_extra_config(name, scenes_data, batches, tuning, steps, warmup, train=None,
+                     single_orders=False):
     """views/s of one configuration under the batched path (CUDA-graph replay)
     with each raster order, and of the plain single-view path (fused rebin,
-    16x16 tiles, row-major), with per-stage times and the learned order's
-    gate state.  Every step renders every view once."""
+    16x16 tiles, row-major; every order with single_orders), with per-stage
+    times and the learned order's gate state.  Every step renders every view
+    once.  train = (uniforms, width, height): the cost model is trained on
+    those poses of the first scene by the library's kernels and installed,
+    instead of the committed checkpoint."""
     import torch
 
     from gs3d import _lib
@@ -702,8 +720,27 @@ def run_extra_config(name, scenes_data, batches, tuning, steps, warmup):
     res = {"views": n_views, "batches": [len(a) for a in arrs],
            "tuning": {"tile": tuned.tile_w, "digit_bits": tuned.digit_bits,
                       "raster_batch": tuned.raster_batch}}
-    learned_sched, model = install_cost_model(lib, ctx, tuned.tile_w)
-    res["cost_model_checkpoint"] = "trained on the 3M-splat 1080p workload" if model else None
+    if train is None:
+        learned_sched, model = install_cost_model(lib, ctx, tuned.tile_w)
+        res["cost_model_checkpoint"] = "trained on the 3M-splat 1080p workload" if model else None
+    else:
+        from gs3d import learned
+        tu, tw, th = train
+        x, t, k = learned.collect(lib, ctx, tu, tw, th)
+        n_fit = len(tu) * 5 // 6
+        fit = learned.train(lib, x[:n_fit].reshape(-1, 16), t[:n_fit].reshape(-1), steps=2000,
+                            batch=65536, lr=5e-3)
+        res["cost_model_heldout"] = {k_: round(float(v), 4) for k_, v in
+                                     learned.evaluate(lib, fit, x[n_fit:], t[n_fit:],
+                                                      k[n_fit:]).items()}
+        f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+        check(lib.gs3d_set_cost_model(ctx, ptr(f32(fit.params)), ptr(f32(fit.mean)),
+                                      ptr(f32(fit.std))))
+        check(lib.gs3d_set_schedule_gate(ctx, C.c_float(learned.ERROR_BOUND)))
+        learned_sched = _lib.SCHEDULE_LEARNED
+        res["cost_model_checkpoint"] = (f"trained in this run on {len(tu)} poses of the "
+                                        "workload (library kernels)")
+        del x, t, k
     # CUDA-graph replay where every batch has one layout (a graph is captured
     # per layout; alternating layouts would re-capture every call)
     graph = len(arrs) == 1
@@ -717,6 +754,9 @@ def run_extra_config(name, scenes_data, batches, tuning, steps, warmup):
         res[label] = timed(False, sc, graph)
     check(lib.gs3d_set_tuning(ctx, C.byref(_lib.Tuning_t(16, 16, 8, 0))))
     res["single_view_fused_16x16_row_major"] = timed(True, _lib.SCHEDULE_ROW_MAJOR, False)
+    if single_orders:
+        res["single_view_fused_16x16_key_count"] = timed(True, _lib.SCHEDULE_KEY_COUNT, False)
+        res["single_view_fused_16x16_learned"] = timed(True, learned_sched, False)
     lib.gs3d_destroy(ctx)
     del stream
     torch.cuda.empty_cache()
@@ -732,7 +772,12 @@ def run_extras(args):
     scs, batches = c4_workload()
     c4 = run_extra_config("skewed stress (10M, 16 4K views)", scs, batches, (32, 32, 8, 512),
                           args.extra_steps, 1)
-    return {"batched_4_scenes_32_mixed_views": c2, "skewed_10M_16_views_4k": c4}
+    del scs
+    scs, batches, train = tail_workload()
+    tail = run_extra_config("tail-bound (opacity mix, 1080p)", scs, batches, (16, 16, 8, 0),
+                            args.extra_steps, 1, train=train, single_orders=True)
+    return {"batched_4_scenes_32_mixed_views": c2, "skewed_10M_16_views_4k": c4,
+            "tail_bound_opacity_mix_1080p_16x16": tail}
 
 
 def profile_run(args):
