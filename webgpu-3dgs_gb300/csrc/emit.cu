@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kThreads)
   // [global tile of the rectangle's first tile, depth bits, splat-view id, -]
   __shared__ uint4 s_ra[kThreads], s_rb[kThreads];
   __shared__ uint32_t s_hist[TP > 0 ? TP : 1][BINS];
-  __shared__ uint32_t s_chunk;
+  __shared__ uint32_t s_first, s_next;  // tickets: the block's first chunk, its next one
 
   const uint32_t total = *ref_counter;
   if (total > capacity) {
@@ -128,12 +128,25 @@ __global__ void __launch_bounds__(kThreads)
   const uint32_t mk[4] = {masks.x, masks.y, masks.z, masks.w};
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t chunks = (n + kThreads - 1) / kThreads;
-  for (;;) {
-    if (threadIdx.x == 0) s_chunk = atomicAdd(chunk_ticket, 1u);
-    // also: the previous chunk's readers are done with s_off / s_ra / s_rb
-    __syncthreads();
-    const uint32_t chunk = s_chunk;
-    if (chunk >= chunks) break;
+  // The next chunk's ticket and its sorted ids, depth keys and offsets are
+  // fetched while the current chunk expands, so a chunk starts with only the
+  // rectangle gather outstanding.
+  uint32_t p_id = 0, p_key = 0, p_off = 0, p_end = 0;
+  auto fetch = [&](uint32_t c) {
+    const uint32_t i = c * kThreads + threadIdx.x;
+    if (c < chunks && i < n) {
+      p_id = __ldg(sorted_ids + i);
+      p_key = __ldg(sorted_keys + i);
+      p_off = __ldg(sorted_offsets + i);
+    }
+    if (threadIdx.x == 0 && c < chunks) p_end = __ldg(sorted_offsets + min(n, (c + 1) * kThreads));
+  };
+  if (threadIdx.x == 0) s_first = atomicAdd(chunk_ticket, 1u);
+  __syncthreads();
+  uint32_t chunk = s_first;
+  fetch(chunk);
+  while (chunk < chunks) {
+    if (threadIdx.x == 0) s_next = atomicAdd(chunk_ticket, 1u);
     const uint32_t first = chunk * kThreads;
     const uint32_t i = first + threadIdx.x;
     if (i < n) {
@@ -142,7 +155,7 @@ __global__ void __launch_bounds__(kThreads)
       // the scan's offsets (0 for culled splats, whose rectangle is zeroed)
       // (or, where every view's tile grid fits 8 bits, the 4-byte word of the
       // preprocess's compact rectangle array, which stays in L2)
-      const uint32_t id = __ldg(sorted_ids + i);
+      const uint32_t id = p_id;
       uint32_t x0, y0, w, h;
       if (rect8 != nullptr) {
         const uint32_t rr = __ldg(rect8 + id);
@@ -159,83 +172,87 @@ __global__ void __launch_bounds__(kThreads)
       }
       const uint32_t v =
           find_view(n_views, id, [&](uint32_t k) { return __ldg(&views[k].splat_base); });
-      s_off[threadIdx.x] = __ldg(sorted_offsets + i);
+      s_off[threadIdx.x] = p_off;
       const uint32_t tx = __ldg(&views[v].f.tile_count[0]);
       // ref k of the splat: row = k / w, tile = first + row * tx + (k - row * w)
       //                                      = first + row * (tx - w) + k
       s_ra[threadIdx.x] = make_uint4(w * h, w, __float_as_uint(1.0f / (float)w), tx - w);
-      s_rb[threadIdx.x] = make_uint4(__ldg(&views[v].f.tile_base) + y0 * tx + x0,
-                                     __ldg(sorted_keys + i), id, 0u);
+      s_rb[threadIdx.x] = make_uint4(__ldg(&views[v].f.tile_base) + y0 * tx + x0, p_key, id, 0u);
     }
     const uint32_t last = min(n, first + kThreads);
-    if (threadIdx.x == 0) s_off[last - first] = __ldg(sorted_offsets + last);
-    __syncthreads();
+    if (threadIdx.x == 0) s_off[last - first] = p_end;
+    __syncthreads();  // the chunk's fields and the next ticket are in shared memory
+    const uint32_t next = s_next;
+    fetch(next);
 
     const uint32_t nloc = last - first;
     const uint32_t begin = s_off[0], end = s_off[nloc];
-    if (end < begin || end > total) {  // block-uniform (shared values): skip the chunk
+    // block-uniform (shared values): an inconsistent chunk is skipped
+    if (end < begin || end > total) {
       if (threadIdx.x == 0) latch_error(err, DEVERR_RANGE);
-      continue;
-    }
-    // Each warp expands a contiguous share of the block's refs, 32 at a time.
-    // The owner of a ref is the last splat starting at or before it.  The
-    // owners of a 32-ref chunk are the owner c0 of its first ref and the
-    // splats c0+1 .. c0+32 starting inside it; while those starts are
-    // distinct (every valid splat has a ref, and culled splats, which have
-    // none, sort after all valid ones) one OR-reduction of their start bits
-    // gives every lane its owner.  A chunk with equal starts (zero-count
-    // splats) searches per ref instead.
-    const uint32_t share = ((end - begin + kThreads - 1) / kThreads) * 32u;
-    const uint32_t wbeg = min(end, begin + warp * share), wend = min(end, wbeg + share);
-    uint32_t c0 = 0;  // owner of ref wbeg: the last splat starting at or before it
-    {
-      uint32_t lo = 0, hi = nloc;  // invariant: s_off[lo] <= wbeg < s_off[hi]
-      while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (s_off[mid] <= wbeg) lo = mid; else hi = mid;
-      }
-      c0 = lo;
-    }
-    for (uint32_t cb = wbeg; cb < wend; cb += 32) {  // warp-uniform trip count
-      const uint32_t j = cb + lane;
-      const uint32_t cand = c0 + 1 + lane;
-      const uint32_t st = cand <= nloc ? s_off[cand] : 0xffffffffu;
-      const uint32_t rel = st - cb;
-      const uint32_t down = __shfl_down_sync(0xffffffffu, st, 1);
-      const uint32_t next_st = lane < 31 ? down : (cand < nloc ? s_off[cand + 1] : 0xffffffffu);
-      uint32_t o;
-      if (!__any_sync(0xffffffffu, rel < 32 && next_st == st)) {
-        const uint32_t starts = __reduce_or_sync(0xffffffffu, rel < 32 ? 1u << rel : 0u);
-        o = c0 + __popc(starts & (0xffffffffu >> (31 - lane)));
-      } else {
-        uint32_t lo = c0, hi = nloc;  // s_off[c0] <= cb <= j
+    } else {
+      // Each warp expands a contiguous share of the block's refs, 32 at a time.
+      // The owner of a ref is the last splat starting at or before it.  The
+      // owners of a 32-ref chunk are the owner c0 of its first ref and the
+      // splats c0+1 .. c0+32 starting inside it; while those starts are
+      // distinct (every valid splat has a ref, and culled splats, which have
+      // none, sort after all valid ones) one OR-reduction of their start bits
+      // gives every lane its owner.  A chunk with equal starts (zero-count
+      // splats) searches per ref instead.
+      const uint32_t share = ((end - begin + kThreads - 1) / kThreads) * 32u;
+      const uint32_t wbeg = min(end, begin + warp * share), wend = min(end, wbeg + share);
+      uint32_t c0 = 0;  // owner of ref wbeg: the last splat starting at or before it
+      {
+        uint32_t lo = 0, hi = nloc;  // invariant: s_off[lo] <= wbeg < s_off[hi]
         while (hi - lo > 1) {
           const uint32_t mid = (lo + hi) >> 1;
-          if (s_off[mid] <= j) lo = mid; else hi = mid;
+          if (s_off[mid] <= wbeg) lo = mid; else hi = mid;
         }
-        o = lo;
+        c0 = lo;
       }
-      c0 = __shfl_sync(0xffffffffu, o, 31);  // owner of the chunk's last ref
-      bool live = j < wend;
-      uint32_t tile = 0;
-      if (live) {
-        const uint32_t k = j - s_off[o];
-        const uint4 ra = s_ra[o];
-        if (k < ra.x) {
-          // row = floor(k / w) by a float reciprocal: exact while k + w < 2^22
-          // (k < w * h <= tiles of one view)
-          const uint32_t row = (uint32_t)(((float)k + 0.5f) * __uint_as_float(ra.z));
-          const uint4 rb = s_rb[o];
-          tile = rb.x + row * ra.w + k;
-          keys[j] = make_uint2(tile, rb.y);
-          values[j] = rb.z;
+      for (uint32_t cb = wbeg; cb < wend; cb += 32) {  // warp-uniform trip count
+        const uint32_t j = cb + lane;
+        const uint32_t cand = c0 + 1 + lane;
+        const uint32_t st = cand <= nloc ? s_off[cand] : 0xffffffffu;
+        const uint32_t rel = st - cb;
+        const uint32_t down = __shfl_down_sync(0xffffffffu, st, 1);
+        const uint32_t next_st = lane < 31 ? down : (cand < nloc ? s_off[cand + 1] : 0xffffffffu);
+        uint32_t o;
+        if (!__any_sync(0xffffffffu, rel < 32 && next_st == st)) {
+          const uint32_t starts = __reduce_or_sync(0xffffffffu, rel < 32 ? 1u << rel : 0u);
+          o = c0 + __popc(starts & (0xffffffffu >> (31 - lane)));
         } else {
-          live = false;
+          uint32_t lo = c0, hi = nloc;  // s_off[c0] <= cb <= j
+          while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (s_off[mid] <= j) lo = mid; else hi = mid;
+          }
+          o = lo;
         }
-      }
+        c0 = __shfl_sync(0xffffffffu, o, 31);  // owner of the chunk's last ref
+        bool live = j < wend;
+        uint32_t tile = 0;
+        if (live) {
+          const uint32_t k = j - s_off[o];
+          const uint4 ra = s_ra[o];
+          if (k < ra.x) {
+            // row = floor(k / w) by a float reciprocal: exact while k + w < 2^22
+            // (k < w * h <= tiles of one view)
+            const uint32_t row = (uint32_t)(((float)k + 0.5f) * __uint_as_float(ra.z));
+            const uint4 rb = s_rb[o];
+            tile = rb.x + row * ra.w + k;
+            keys[j] = make_uint2(tile, rb.y);
+            values[j] = rb.z;
+          } else {
+            live = false;
+          }
+        }
 #pragma unroll
-      for (int p = 0; p < TP; ++p) hist_add_256(s_hist[p], (tile >> sh[p]) & mk[p], live);
+        for (int p = 0; p < TP; ++p) hist_add_256(s_hist[p], (tile >> sh[p]) & mk[p], live);
+      }
     }
+    __syncthreads();  // the chunk's readers are done with its fields and with s_next
+    chunk = next;
   }
   __syncthreads();
   for (int k = threadIdx.x; k < TP * BINS; k += kThreads) {
