@@ -129,9 +129,11 @@ __global__ void __launch_bounds__(kThreads)
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t chunks = (n + kThreads - 1) / kThreads;
   // The next chunk's ticket and its sorted ids, depth keys and offsets are
-  // fetched while the current chunk expands, so a chunk starts with only the
-  // rectangle gather outstanding.
+  // fetched while the current chunk expands, and its rectangles gathered
+  // before the barrier that ends the chunk (while the warps that finished
+  // wait there), so a chunk starts with its fields in registers.
   uint32_t p_id = 0, p_key = 0, p_off = 0, p_end = 0;
+  uint4 p_rect = make_uint4(0u, 0u, 0u, 0u);  // [x0, y0, x1, y1]
   auto fetch = [&](uint32_t c) {
     const uint32_t i = c * kThreads + threadIdx.x;
     if (c < chunks && i < n) {
@@ -141,35 +143,34 @@ __global__ void __launch_bounds__(kThreads)
     }
     if (threadIdx.x == 0 && c < chunks) p_end = __ldg(sorted_offsets + min(n, (c + 1) * kThreads));
   };
+  // only the tile rectangle is gathered (one 32-byte sector of the record):
+  // the depth bits come in order from the depth sort, the ref count from the
+  // scan's offsets (0 for culled splats, whose rectangle is zeroed) (or,
+  // where every view's tile grid fits 8 bits, the 4-byte word of the
+  // preprocess's compact rectangle array, which stays in L2)
+  auto gather = [&](uint32_t c) {
+    if (c >= chunks || c * kThreads + threadIdx.x >= n) return;
+    if (rect8 != nullptr) {
+      const uint32_t rr = __ldg(rect8 + p_id);
+      const uint32_t x0 = rr & 0xffu, y0 = (rr >> 8) & 0xffu;
+      p_rect = make_uint4(x0, y0, x0 + ((rr >> 16) & 0xffu), y0 + (rr >> 24));
+    } else {
+      p_rect = __ldg(reinterpret_cast<const uint4*>(proj + p_id) + 3);
+    }
+  };
   if (threadIdx.x == 0) s_first = atomicAdd(chunk_ticket, 1u);
   __syncthreads();
   uint32_t chunk = s_first;
   fetch(chunk);
+  gather(chunk);
   while (chunk < chunks) {
     if (threadIdx.x == 0) s_next = atomicAdd(chunk_ticket, 1u);
     const uint32_t first = chunk * kThreads;
     const uint32_t i = first + threadIdx.x;
     if (i < n) {
-      // only the tile rectangle is gathered (one 32-byte sector of the record):
-      // the depth bits come in order from the depth sort, the ref count from
-      // the scan's offsets (0 for culled splats, whose rectangle is zeroed)
-      // (or, where every view's tile grid fits 8 bits, the 4-byte word of the
-      // preprocess's compact rectangle array, which stays in L2)
       const uint32_t id = p_id;
-      uint32_t x0, y0, w, h;
-      if (rect8 != nullptr) {
-        const uint32_t rr = __ldg(rect8 + id);
-        x0 = rr & 0xffu;
-        y0 = (rr >> 8) & 0xffu;
-        w = ((rr >> 16) & 0xffu) + 1u;
-        h = (rr >> 24) + 1u;
-      } else {
-        const uint4 r3 = __ldg(reinterpret_cast<const uint4*>(proj + id) + 3);
-        x0 = r3.x;
-        y0 = r3.y;
-        w = r3.z - r3.x + 1u;
-        h = r3.w - r3.y + 1u;
-      }
+      const uint32_t x0 = p_rect.x, y0 = p_rect.y;
+      const uint32_t w = p_rect.z - p_rect.x + 1u, h = p_rect.w - p_rect.y + 1u;
       const uint32_t v =
           find_view(n_views, id, [&](uint32_t k) { return __ldg(&views[k].splat_base); });
       s_off[threadIdx.x] = p_off;
@@ -251,6 +252,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int p = 0; p < TP; ++p) hist_add_256(s_hist[p], (tile >> sh[p]) & mk[p], live);
       }
     }
+    gather(next);
     __syncthreads();  // the chunk's readers are done with its fields and with s_next
     chunk = next;
   }
