@@ -34,7 +34,8 @@ using namespace gs3d;
 
 namespace {
 
-// Refs are indexed by u32 and key buffers hold whole 4096-key partitions.
+// Refs are indexed by u32 and key buffers hold whole 12288-key blocks (the
+// 4096- and 6144-key partitions of the sort passes).
 constexpr uint32_t kMaxCapacity = 0xFFFFE000u;
 constexpr int kUploadSlots = 8;
 constexpr uint32_t kPreBlock = 256;  // preprocess threads per block

@@ -284,8 +284,8 @@ size_t sort_status_words(uint32_t capacity, int passes);
 // Status words any sort plan of a capacity needs (11-bit tile passes included).
 size_t sort_status_words_max(uint32_t capacity);
 // Key/value buffers handed to the sort must hold this many entries: passes
-// always fetch whole 4096-key partitions (entries past the live count are
-// read and ignored).
+// always fetch whole partitions, 4096 keys of 8 bytes or 6144 of 4 bytes
+// (entries past the live count are read and ignored).
 uint32_t sort_capacity_round(uint32_t capacity);
 // Tile-id passes of the fused rebin: histograms already in
 // g_hist[p * kTileHistStride + digit].

@@ -8,7 +8,8 @@
 //   1. one histogram kernel reads every key once and builds the 256-bin
 //      histogram of every digit place that is sorted (and clears the
 //      look-back status of the passes);
-//   2. one kernel per pass: a persistent CTA claims 4096-key partitions in
+//   2. one kernel per pass: a persistent CTA claims partitions (4096 8-byte
+//      or 6144 4-byte keys) in
 //      order, ranks its keys stably with warp ballots (8 ballots give each
 //      lane the mask of lanes holding the same 8-bit digit) and per-warp
 //      shared-memory histograms, publishes its per-digit counts, resolves
@@ -41,9 +42,10 @@ constexpr int kHistItems = 16;  // keys a histogram thread loads per round
 constexpr int kPassThreads = 512;                  // onesweep pass (8-bit and narrower digits)
 constexpr int kWarps = kPassThreads / 32;          // 16
 constexpr int kItems = 8;
-constexpr uint32_t kPart = kPassThreads * kItems;  // 4096 keys per partition
-// key buffers are padded to whole partitions of every pass kernel
-constexpr uint32_t kRoundPart = 4096;
+constexpr uint32_t kPart = kPassThreads * kItems;  // 4096 keys per partition (uint2 keys)
+// key buffers are padded to whole partitions of every pass kernel (4096 and
+// 6144 keys)
+constexpr uint32_t kRoundPart = 12288;
 constexpr uint32_t kFlagAgg = 1u, kFlagInc = 2u;
 constexpr uint32_t kValueMask = (1u << 30) - 1u;
 constexpr int kLookback = 16;  // predecessor status words fetched per look-back step
@@ -65,9 +67,27 @@ struct KeyOps<uint32_t> {
   }
 };
 
+// Keys a pass thread ranks per partition.  A partition costs about the same
+// time whatever its keys' width (ranking, barriers and the look-back's L2
+// round trips dominate), so 4-byte keys take 12 a thread: their 6144-key
+// partitions fill the 48 KB buffer of a 4096-key partition of 8-byte keys,
+// and two CTAs still fit an SM.
+template <typename K>
+struct PassItems {
+  static constexpr int value = 8;
+};
+template <>
+struct PassItems<uint32_t> {
+  static constexpr int value = 12;
+};
+template <typename K>
+constexpr uint32_t pass_part() {
+  return kPassThreads * (uint32_t)PassItems<K>::value;
+}
+
 template <typename K>
 constexpr size_t pass_smem() {  // two partition buffers + per-warp u16 histograms
-  return 2 * (size_t)kPart * (sizeof(K) + sizeof(uint32_t)) +
+  return 2 * (size_t)pass_part<K>() * (sizeof(K) + sizeof(uint32_t)) +
          (size_t)kWarps * kRadixBins * sizeof(uint16_t);
 }
 
@@ -174,7 +194,7 @@ __global__ void __launch_bounds__(kThreads)
 
 template <typename K>
 constexpr size_t part_buf_bytes() {
-  return (size_t)kPart * (sizeof(K) + sizeof(uint32_t));
+  return (size_t)pass_part<K>() * (sizeof(K) + sizeof(uint32_t));
 }
 
 // Inclusive scan over lanes 0..7 (the eight digit warps' totals).
@@ -187,7 +207,7 @@ __device__ __forceinline__ uint32_t scan8_inclusive(uint32_t x, int lane) {
   return x;
 }
 
-// One LSD pass.  Persistent CTAs claim 4096-key partitions in order.  A
+// One LSD pass.  Persistent CTAs claim partitions in order (pass_part).  A
 // partition is claimed when the CTA has resolved its current one (barrier C
 // below), and fetched by two bulk (TMA) copies into the other shared-memory
 // buffer while the current partition is written out; the claimed partition's
@@ -216,6 +236,8 @@ __global__ void __launch_bounds__(kPassThreads, 1024 / kPassThreads)
                     uint32_t* __restrict__ part_counter, uint32_t* __restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr size_t kBuf = part_buf_bytes<K>();
+  constexpr int kI = PassItems<K>::value;   // keys a thread ranks
+  constexpr uint32_t kP = pass_part<K>();   // keys a partition holds
   // [kWarps][256] per-warp digit counts, then per-warp exclusive offsets
   uint16_t* s_whist = reinterpret_cast<uint16_t*>(smem + 2 * kBuf);
   __shared__ uint32_t s_bucket[kRadixBins], s_dloc[kRadixBins], s_dest[kRadixBins];
@@ -229,7 +251,7 @@ __global__ void __launch_bounds__(kPassThreads, 1024 / kPassThreads)
   }
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t R = live_refs(ref_counter, capacity);
-  const uint32_t num_parts = (R + kPart - 1) / kPart;
+  const uint32_t num_parts = (R + kP - 1) / kP;
   // digits are NBITS wide; the all-ones sentinel of the tail items maps to
   // the largest digit and ranks after every real item of it
   constexpr uint32_t kDigitMask = NBITS >= 8 ? 0xffu : ((1u << NBITS) - 1u);
@@ -242,11 +264,11 @@ __global__ void __launch_bounds__(kPassThreads, 1024 / kPassThreads)
     s_part[b] = part;  // published by the arrive below (release)
     if (part < num_parts) {
       unsigned char* buf = smem + b * kBuf;
-      const uint32_t kb = kPart * sizeof(K), vb = kPart * sizeof(uint32_t);
+      const uint32_t kb = kP * sizeof(K), vb = kP * sizeof(uint32_t);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_expect_tx(&s_bar[b], kb + vb);
-      bulk_g2s(buf, keys_in + (size_t)part * kPart, kb, &s_bar[b]);
-      bulk_g2s(buf + kb, vals_in + (size_t)part * kPart, vb, &s_bar[b]);
+      bulk_g2s(buf, keys_in + (size_t)part * kP, kb, &s_bar[b]);
+      bulk_g2s(buf + kb, vals_in + (size_t)part * kP, vb, &s_bar[b]);
     } else {
       mbar_arrive(&s_bar[b]);
     }
@@ -278,19 +300,19 @@ __global__ void __launch_bounds__(kPassThreads, 1024 / kPassThreads)
     reinterpret_cast<uint4*>(wh)[lane] = make_uint4(0u, 0u, 0u, 0u);
     __syncwarp();
     K* s_keys = reinterpret_cast<K*>(smem + b * kBuf);
-    uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + b * kBuf + kPart * sizeof(K));
+    uint32_t* s_vals = reinterpret_cast<uint32_t*>(smem + b * kBuf + kP * sizeof(K));
     const bool landed = mbar_wait(&s_bar[b], b ? phase1 : phase0);
     if (b) phase1 ^= 1u; else phase0 ^= 1u;
     const uint32_t part = landed ? s_part[b] : num_parts;
-    const uint32_t count = part < num_parts ? min(kPart, R - part * kPart) : 0u;
+    const uint32_t count = part < num_parts ? min(kP, R - part * kP) : 0u;
 
     // ---- registers <- shared (warp-striped: lane-contiguous) ----
-    K key[kItems];
-    uint32_t val[kItems];
-    uint32_t dr[kItems];  // digit | rank-in-warp << 8
-    const uint32_t wloc = warp * (32u * kItems);
+    K key[kI];
+    uint32_t val[kI];
+    uint32_t dr[kI];  // digit | rank-in-warp << 8
+    const uint32_t wloc = warp * (32u * kI);
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) {
+    for (int i = 0; i < kI; ++i) {
       const uint32_t loc = wloc + i * 32u + lane;
       if (loc < count) {
         key[i] = s_keys[loc];
@@ -302,7 +324,7 @@ __global__ void __launch_bounds__(kPassThreads, 1024 / kPassThreads)
     }
     // ---- stable rank within the warp ----
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) {
+    for (int i = 0; i < kI; ++i) {
       const uint32_t d = KeyOps<K>::digit(key[i], word, shift) & kDigitMask;
       const uint32_t peers = match_digit<NBITS>(d);
       const uint32_t prior = wh[d];
@@ -331,7 +353,7 @@ __global__ void __launch_bounds__(kPassThreads, 1024 / kPassThreads)
         s_whist[w * kRadixBins + tid] = (uint16_t)run;
         run += t;
       }
-      pub = ((uint32_t)tid == kDigitMask) ? run - (kPart - count) : run;
+      pub = ((uint32_t)tid == kDigitMask) ? run - (kP - count) : run;
       st_relaxed_u32(st, ((part == 0 ? kFlagInc : kFlagAgg) << 30) | pub);
       const uint32_t inc = warp_inclusive(run, lane);
       s_dloc[tid] = inc - run;  // exclusive within the digit warp
@@ -356,7 +378,7 @@ __global__ void __launch_bounds__(kPassThreads, 1024 / kPassThreads)
 
     // ---- reorder the partition in place ----
 #pragma unroll
-    for (int i = 0; i < kItems; ++i) {
+    for (int i = 0; i < kI; ++i) {
       const uint32_t pos = wh[dr[i] & 0xffu] + (dr[i] >> 8);
       s_keys[pos] = key[i];
       s_vals[pos] = val[i];
