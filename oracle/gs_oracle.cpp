@@ -76,7 +76,9 @@ const float SH_C3[7] = {-0.5900435899266435f, 2.890611442640554f,
 // SH colour extension (not in the reference, whose colour is SH degree 0
 // baked at load time, SceneWorker.ts:430-432).  base = splat_colors.rgb;
 // colour_c = clamp01(base_c + sum_k basis_k(dir) * rest[c*K + k-1]) with
-// dir = normalize(position - camera position) and K = (deg+1)^2 - 1.
+// dir = normalize(position - camera position) and K = (deg+1)^2 - 1; the
+// sum runs k = 1..K, each term added by one fused multiply-add (a single
+// rounding, as the GPU's fmaf).
 void sh_color(const float* p, const float* cam_pos, const float* base,
               const float* rest, uint32_t deg, float out[3]) {
   const uint32_t K = (deg + 1) * (deg + 1) - 1;
@@ -114,7 +116,7 @@ void sh_color(const float* p, const float* cam_pos, const float* base,
   }
   for (int c = 0; c < 3; ++c) {
     float acc = base[c];
-    for (uint32_t k = 1; k <= K; ++k) acc = acc + b[k] * rest[c * K + (k - 1)];
+    for (uint32_t k = 1; k <= K; ++k) acc = std::fma(b[k], rest[c * K + (k - 1)], acc);
     out[c] = std::min(1.0f, std::max(0.0f, acc));
   }
 }

@@ -28,7 +28,9 @@ __constant__ float kShC3[7] = {-0.5900435899266435f, 2.890611442640554f, -0.4570
 
 // Colour extension: clamp01(base + sum_k Y_k(dir) * rest[c*K + k-1]), with
 // dir = normalize(position - camera position), K = (DEG+1)^2 - 1 and the
-// rest coefficients in PLY f_rest order (channel-major).
+// rest coefficients in PLY f_rest order (channel-major); the sum runs
+// k = 1..K, each term added by one explicit fused multiply-add (the oracle
+// uses std::fma in the same order).
 template <int DEG>
 __device__ __forceinline__ void sh_color(float px, float py, float pz, const float* campos,
                                          float4 base, const float* rest, float* out) {
@@ -70,7 +72,7 @@ __device__ __forceinline__ void sh_color(float px, float py, float pz, const flo
   for (int c = 0; c < 3; ++c) {
     float acc = base_c[c];
 #pragma unroll
-    for (int k = 1; k <= K; ++k) acc = acc + b[k] * rest[c * K + (k - 1)];
+    for (int k = 1; k <= K; ++k) acc = __fmaf_rn(b[k], rest[c * K + (k - 1)], acc);
     out[c] = fminf(1.0f, fmaxf(0.0f, acc));
   }
 }
