@@ -137,14 +137,22 @@ struct PassDev {
 };
 
 // Histogram of every sorted digit place + clear of the look-back status.
+// The top place (the depth keys' exponent byte: a handful of values) is
+// counted in per-lane sub-histograms 257 words apart, so lanes adding the
+// same digit hit different banks instead of serialising on one word; they
+// are summed at the block's flush.
+constexpr uint32_t kLaneStride = kRadixBins + 1;
 template <typename K, int P>
 __global__ void __launch_bounds__(kThreads)
     sort_histogram_kernel(const K* __restrict__ keys, const uint32_t* __restrict__ ref_counter,
                           uint32_t capacity, PassDev pd, uint32_t* __restrict__ g_hist,
                           uint32_t* __restrict__ status, size_t status_stride) {
   __shared__ uint32_t s_hist[P][kRadixBins];
+  __shared__ uint32_t s_top[32 * kLaneStride];
   for (int k = threadIdx.x; k < P * kRadixBins; k += kThreads) (&s_hist[0][0])[k] = 0u;
+  for (int k = threadIdx.x; k < 32 * (int)kLaneStride; k += kThreads) s_top[k] = 0u;
   __syncthreads();
+  const uint32_t lane_base = (threadIdx.x & 31u) * kLaneStride;
 
   const uint32_t R = live_refs(ref_counter, capacity);
   const size_t parts = (R + kPart - 1) / kPart;
@@ -181,9 +189,19 @@ __global__ void __launch_bounds__(kThreads)
     for (int i = 0; i < kHistItems; ++i) {
       const bool in = base + (size_t)i * kThreads + threadIdx.x < R;
 #pragma unroll
-      for (int p = 0; p < P; ++p)
+      for (int p = 0; p < P - 1; ++p)
         hist_add_256(s_hist[p], KeyOps<K>::digit(k[i], word[p], shift[p]) & mask[p], in);
+      if (in)
+        atomicAdd(s_top + lane_base +
+                      (KeyOps<K>::digit(k[i], word[P - 1], shift[P - 1]) & mask[P - 1]),
+                  1u);
     }
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < (int)kRadixBins; d += kThreads) {
+    uint32_t sum = 0;
+    for (int l = 0; l < 32; ++l) sum += s_top[l * kLaneStride + d];
+    s_hist[P - 1][d] += sum;
   }
   __syncthreads();
   for (int k = threadIdx.x; k < P * kRadixBins; k += kThreads) {
