@@ -224,9 +224,9 @@ def dominant_traffic(stage, tile, refs_per_launch, splats_per_launch, scene_spla
 # Pipe use of the raster kernel (ncu --set full, one launch of the headline
 # path's raster at 32x32 tiles, 2-view batch;
 # profiles/raster_culled2_t32_2views_3M_sh3_1080p.md).
-RASTER_NCU = {"kernel": "raster_kernel_culled2", "issue_active": 0.739, "pipe_fma": 0.443,
-              "pipe_alu": 0.602, "pipe_xu": 0.169, "warps_active": 0.496,
-              "source": "profiles/raster_culled2_t32_2views_3M_sh3_1080p.md"}
+RASTER_NCU = {"kernel": "raster_kernel_culled2", "issue_active": 0.732, "pipe_fma": 0.442,
+              "pipe_alu": 0.589, "pipe_xu": 0.173, "warps_active": 0.497,
+              "source": "profiles/raster_culled2_t32_2views_3M_sh3_1080p.md (raster_t32c)"}
 
 
 def raster_work(view=0, tile=TILE):
