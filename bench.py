@@ -243,12 +243,12 @@ def raster_work(view=0, tile=TILE):
                           r["sort_values_a"])
 
 
-def install_cost_model(lib, ctx, tile):
+def install_cost_model(lib, ctx, tile_w, tile_h=None):
     """Cost model trained for this tile size, behind its gate; returns the
     schedule to use and the model's held-out metrics (None when no model
     exists for the tile size: key counts)."""
     from gs3d import _lib, learned
-    path = learned.checkpoint_for(tile, tile)
+    path = learned.checkpoint_for(tile_w, tile_w if tile_h is None else tile_h)
     if path is None:
         return _lib.SCHEDULE_KEY_COUNT, None
     mp, mmean, mstd, mmetrics, mbound = learned.load(path)
@@ -327,17 +327,19 @@ def run_ours(args, rank, world):
     check(lib.gs3d_set_flags(ctx, 0))
     tuned = _lib.Tuning_t()
     check(lib.gs3d_get_tuning(ctx, C.byref(tuned)))
-    tune_table = sorted(({"tile": r.tuning.tile_w, "digit_bits": r.tuning.digit_bits,
+    tune_table = sorted(({"tile": [r.tuning.tile_w, r.tuning.tile_h],
+                          "digit_bits": r.tuning.digit_bits,
                           "raster_batch": r.tuning.raster_batch,
                           "ms_per_view": round(float(r.ms_per_view), 4),
                           "tile_passes": int(r.tile_passes)}
                          for r in tune_out[:n_tuned.value]), key=lambda r: r["ms_per_view"])
     best = next(r for r in tune_out[:n_tuned.value]
-                if (r.tuning.tile_w, r.tuning.digit_bits, r.tuning.raster_batch) ==
-                (tuned.tile_w, tuned.digit_bits, tuned.raster_batch))
+                if (r.tuning.tile_w, r.tuning.tile_h, r.tuning.digit_bits,
+                    r.tuning.raster_batch) ==
+                (tuned.tile_w, tuned.tile_h, tuned.digit_bits, tuned.raster_batch))
     tuned_R = best.refs / len(batches[0])
     tuned_passes = int(best.tile_passes)
-    batched_schedule, tuned_model = install_cost_model(lib, ctx, tuned.tile_w)
+    batched_schedule, tuned_model = install_cost_model(lib, ctx, tuned.tile_w, tuned.tile_h)
 
     def run_step(path):
         if path == "batched":
@@ -548,7 +550,7 @@ def run_ours(args, rank, world):
         "schedules": sched_raster, "schedules_batched": sched_batched,
         "learned_active": learned_on, "best_order": best_order,
         "cost_model": {k: round(v, 4) for k, v in (tuned_model or {}).items()},
-        "tuning": {"tile": tuned.tile_w, "digit_bits": tuned.digit_bits,
+        "tuning": {"tile": [tuned.tile_w, tuned.tile_h], "digit_bits": tuned.digit_bits,
                    "raster_batch": tuned.raster_batch, "candidates": tune_table},
         "tile_passes_batched": tuned_passes,
         "traffic": dominant_traffic(dom, tuned.tile_w, tuned_R * B, N_SPLATS * B, N_SPLATS),
@@ -718,10 +720,10 @@ def run_extra_config(name, scenes_data, batches, tuning, steps, warmup, train=No
                 if schedule == _lib.SCHEDULE_LEARNED else None}
 
     res = {"views": n_views, "batches": [len(a) for a in arrs],
-           "tuning": {"tile": tuned.tile_w, "digit_bits": tuned.digit_bits,
+           "tuning": {"tile": [tuned.tile_w, tuned.tile_h], "digit_bits": tuned.digit_bits,
                       "raster_batch": tuned.raster_batch}}
     if train is None:
-        learned_sched, model = install_cost_model(lib, ctx, tuned.tile_w)
+        learned_sched, model = install_cost_model(lib, ctx, tuned.tile_w, tuned.tile_h)
         res["cost_model_checkpoint"] = "trained on the 3M-splat 1080p workload" if model else None
     else:
         from gs3d import learned
@@ -794,11 +796,13 @@ def profile_run(args):
     assert lib.gs3d_set_splats(ctx, data.splatCount, ptr(data.positions), ptr(data.scales),
                                ptr(data.rotations), ptr(data.colors),
                                ptr(data.sphericalHarmonics), 3, 0) == 0
-    tile, digit_bits, raster_batch = (int(x) for x in args.tuning.split(","))
-    assert lib.gs3d_set_tuning(ctx, C.byref(_lib.Tuning_t(tile, tile, digit_bits,
+    tile_s, digit_s, batch_s = args.tuning.split(",")
+    tile_w, tile_h = (int(x) for x in tile_s.split("x")) if "x" in tile_s else (int(tile_s),) * 2
+    digit_bits, raster_batch = int(digit_s), int(batch_s)
+    assert lib.gs3d_set_tuning(ctx, C.byref(_lib.Tuning_t(tile_w, tile_h, digit_bits,
                                                            raster_batch))) == 0
     if args.order == "learned":
-        schedule, _ = install_cost_model(lib, ctx, tile)
+        schedule, _ = install_cost_model(lib, ctx, tile_w, tile_h)
     else:
         schedule = {"row_major": _lib.SCHEDULE_ROW_MAJOR,
                     "key_count": _lib.SCHEDULE_KEY_COUNT}[args.order]
@@ -852,7 +856,8 @@ def main():
                     help="profiling run: render STEPS batched steps of --views views and exit "
                          "(no timing, no JSON)")
     ap.add_argument("--tuning", default=f"{TILE},8,0", metavar="TILE,DIGIT_BITS,RASTER_BATCH",
-                    help="profiling run: the tuning to render with (the bench autotunes)")
+                    help="profiling run: the tuning to render with, TILE square or WxH "
+                         "(the bench autotunes)")
     ap.add_argument("--order", default="key_count", choices=["row_major", "key_count", "learned"],
                     help="profiling run: the raster order")
     args = ap.parse_args()

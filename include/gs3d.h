@@ -275,12 +275,15 @@ int gs3d_set_schedule(struct gs3d_ctx* ctx, uint32_t schedule);
  * the tile grid), while the tile grid, key layout and tile_offsets follow
  * tile_w x tile_h. */
 typedef struct gs3d_tuning {
-    uint32_t tile_w, tile_h;  /* tile pixel size (gs3d_set_tile_size)                 */
+    uint32_t tile_w, tile_h;  /* tile pixel size: up to 1024 pixels, or up to 2048
+                                 with tile_w a multiple of 8 and tile_h of 16 (such
+                                 tiles are shaded by the culled two-pixel raster
+                                 only: the stage-wise rebin rejects them)             */
     uint32_t digit_bits;      /* widest radix digit of the tile-id passes: 4, 6, 8 or
                                  11 (fused rebin; the stage-wise sort uses at most 8);
                                  8 when narrower digits would need over 4 passes     */
     uint32_t raster_batch;    /* splats staged per raster batch: a multiple of 32 in
-                                 [32, 1024]; 0 = one per tile pixel                   */
+                                 [32, 1024]; 0 = one per tile pixel (at most 1024)    */
 } gs3d_tuning;
 
 typedef struct gs3d_tune_result {
@@ -295,8 +298,8 @@ int gs3d_get_tuning(struct gs3d_ctx* ctx, gs3d_tuning* out);
 
 /* Autotuner: times the batched rebin of `views` (warm-up, then `reps` timed
  * repetitions, CUDA events on the context's stream) under every candidate
- * of tile size {8, 16, 32} square x digit width {4, 8, 11} x raster batch
- * {128, 256, 512}, applies the fastest and writes up to max_results
+ * of tile size {8x8, 16x16, 32x32, 32x64, 64x32} x digit width {4, 8, 11} x
+ * raster batch {128, 256, 512}, applies the fastest and writes up to max_results
  * measurements (n_results = candidates measured; candidates whose refs
  * exceed the 2^30 limit of one rebin are skipped).  Blocking. */
 int gs3d_autotune(struct gs3d_ctx* ctx, const gs3d_view* views, uint32_t n_views,

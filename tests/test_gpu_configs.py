@@ -70,8 +70,15 @@ def test_batched_config_full_size(renderer):
     assert (best["tile"], best["digit_bits"], best["raster_batch"]) == \
         (res[0]["tile"], res[0]["digit_bits"], res[0]["raster_batch"])
     r.rebinBatch(views)
-    # global tile ids: the view folded into the key's high bits
-    assert r.viewInfo(31).tile_base > 2 ** 16
+    # global tile ids: every view's grid follows the previous views' grids, so
+    # the view is folded into the key's high bits
+    base = 0
+    for v in range(len(views)):
+        info = r.viewInfo(v)
+        assert info.tile_base == base
+        base += info.tiles_x * info.tiles_y
+    assert r.viewInfo(31).tile_base > 31 * min(r.viewInfo(v).tiles_x * r.viewInfo(v).tiles_y
+                                               for v in range(31))
     # one view of each scene, including the 4K ones
     picks = {}
     for v, (sid, _, w, h) in enumerate(views):

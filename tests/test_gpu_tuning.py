@@ -36,7 +36,7 @@ def test_every_tuning_renders_the_same_image(renderer):
     renderer.setTuning(16, 8, 0)
     renderer.rebinBatch(views)
     want = _images(renderer, views)
-    for tile in (8, 16, 32):
+    for tile in (8, 16, 32, (32, 64), (64, 32)):
         for digit in (4, 6, 8, 11):
             for batch in (0, 64, 512):
                 renderer.setTuning(tile, digit, batch)
@@ -78,6 +78,43 @@ def test_tuned_keys_match_the_oracle(renderer, oracle, tile, digit, batch):
     renderer.setTuning(16, 8, 0)
 
 
+@pytest.mark.parametrize("tw,th,digit,batch", [(32, 64, 8, 256), (64, 32, 8, 0),
+                                                (128, 16, 6, 512), (32, 64, 11, 128)])
+def test_wide_tiles_match_the_oracle(renderer, oracle, tw, th, digit, batch):
+    """2048-pixel tiles (tuning API only: shaded by the two-pixel raster as
+    row strips of at most 512 threads): keys, values and tile ranges
+    bit-exact with the oracle's for that grid, the image within tolerance,
+    tile costs as the oracle counts them."""
+    data = scenes.scene_small(60_000, seed=11)
+    w, h = 1000, 563
+    u = scenes.small_camera(w, h).getUniformData(w, h)
+    o = oracle.rebin(u, w, h, tw, th, data.positions, data.scales, data.rotations,
+                     data.colors, data.sphericalHarmonics, data.sphericalHarmonicsDegree)
+    renderer.setSplatData(data)
+    renderer.setTuning((tw, th), digit, batch)
+    try:
+        renderer.rebin(data.splatCount, -(-w // tw), -(-h // th), w, h, u)
+        R = renderer.refCount()
+        assert R == o["ref_counter"]
+        assert np.array_equal(renderer.readBuffer("sort_keys_a", R), o["sort_keys_a"])
+        assert np.array_equal(renderer.readBuffer("sort_values_a", R), o["sort_values_a"])
+        assert np.array_equal(renderer.readBuffer("tile_offsets"), o["tile_offsets"])
+        img = renderer.readImage().astype(np.float32)
+        assert np.abs(img - o["image"]).max() <= 2.0 / 255.0
+        gc = renderer.readBuffer("tile_costs").astype(np.int64)
+        oc = o["tile_costs"].astype(np.int64)
+        assert np.mean(gc == oc) >= 0.98
+        assert np.abs(gc - oc).sum() <= 0.01 * max(1, oc.sum())
+        # the stage-wise rebin's one-pixel raster cannot shade them
+        renderer.setStagewise(True)
+        with pytest.raises(Gs3dError) as ei:
+            renderer.rebin(data.splatCount, -(-w // tw), -(-h // th), w, h, u)
+        assert ei.value.code == _lib.ERR_INVALID_ARG
+    finally:
+        renderer.setStagewise(False)
+        renderer.setTuning(16, 8, 0)
+
+
 @pytest.mark.parametrize("w,h", [(2048, 300), (2400, 300), (300, 2100)])
 def test_tile_grids_wider_than_256_match_the_oracle(renderer, oracle, w, h):
     """Grids of more than 256 tiles on an axis keep the emit's tile
@@ -117,7 +154,7 @@ def test_autotune_applies_the_fastest_candidate(renderer):
     renderer.rebinBatch(views)
     want = _images(renderer, views)
     res = renderer.autotune(views, reps=2)
-    assert len(res) == 3 * 3 * 3
+    assert len(res) == 5 * 3 * 3
     assert all(r["ms_per_view"] > 0 for r in res)
     best = renderer.getTuning()
     assert (best["tile"], best["digit_bits"], best["raster_batch"]) == \
@@ -135,7 +172,8 @@ def test_autotune_applies_the_fastest_candidate(renderer):
 
 
 def test_bad_tunings_are_rejected(renderer):
-    for bad in [(16, 7, 0), (16, 12, 0), (16, 8, 48), (16, 8, 2048), (64, 8, 0)]:
+    for bad in [(16, 7, 0), (16, 12, 0), (16, 8, 48), (16, 8, 2048), (64, 8, 0),
+                ((64, 24), 8, 0), ((60, 32), 8, 0), ((128, 32), 8, 0)]:
         with pytest.raises(Gs3dError) as ei:
             renderer.setTuning(*bad)
         assert ei.value.code == _lib.ERR_INVALID_ARG

@@ -503,6 +503,11 @@ SortPlan tile_digit_plan(uint32_t num_tiles, uint32_t digit_bits) {
 }
 
 int raster_stage(gs3d_ctx* c, bool culled) {
+  if ((uint64_t)c->tile_w * c->tile_h > 1024 && !culled)
+    return fail(c, GS3D_ERR_INVALID_ARG,
+                "tiles of %ux%u pixels are shaded by the culled two-pixel raster only; the "
+                "stage-wise rebin's one-pixel raster takes at most 1024",
+                c->tile_w, c->tile_h);
   StageScope t(c, GS3D_STAGE_RASTER);
   RasterArgs a{};
   a.views = dviews(c);
@@ -510,7 +515,10 @@ int raster_stage(gs3d_ctx* c, bool culled) {
   a.num_tiles = c->total_tiles;
   a.tile_w = c->tile_w;
   a.tile_h = c->tile_h;
-  a.batch = c->raster_batch;
+  // raster_batch 0 stages one splat per tile pixel, at most 1024 (the staged
+  // batches of a 2048-pixel tile would not fit shared memory)
+  a.batch = c->raster_batch ? c->raster_batch
+                            : ((uint64_t)c->tile_w * c->tile_h > 1024 ? 1024u : 0u);
   a.culled = culled;
   uint32_t strips = 1, raster_ctas = 1;
   CK(raster_shape(a, c->sm_count, &strips, &raster_ctas), "raster shape");
@@ -1016,16 +1024,22 @@ int gs3d_load_ply(gs3d_ctx* c, const void* data, size_t size, uint32_t target,
   return GS3D_OK;
 }
 
-int gs3d_set_tile_size(gs3d_ctx* c, uint32_t tx, uint32_t ty, uint32_t* out_x, uint32_t* out_y) {
-  if (!c) return GS3D_ERR_INVALID_ARG;
-  // clampTileSize (GaussianSplatRenderer.ts:162-167) with CUDA's 1024-thread block limit
-  tx = std::max<uint32_t>(1, std::min<uint32_t>(tx ? tx : 1, 1024));
-  ty = std::max<uint32_t>(1, std::min<uint32_t>(ty ? ty : 1, 1024 / tx));
+namespace {
+void apply_tile_size(gs3d_ctx* c, uint32_t tx, uint32_t ty) {
   if (tx != c->tile_w || ty != c->tile_h) {
     c->tile_w = tx;
     c->tile_h = ty;
     c->have_camera = false;  // tile grid recomputed at the next set_camera
   }
+}
+}  // namespace
+
+int gs3d_set_tile_size(gs3d_ctx* c, uint32_t tx, uint32_t ty, uint32_t* out_x, uint32_t* out_y) {
+  if (!c) return GS3D_ERR_INVALID_ARG;
+  // clampTileSize (GaussianSplatRenderer.ts:162-167) with CUDA's 1024-thread block limit
+  tx = std::max<uint32_t>(1, std::min<uint32_t>(tx ? tx : 1, 1024));
+  ty = std::max<uint32_t>(1, std::min<uint32_t>(ty ? ty : 1, 1024 / tx));
+  apply_tile_size(c, tx, ty);
   if (out_x) *out_x = tx;
   if (out_y) *out_y = ty;
   return GS3D_OK;
@@ -1181,9 +1195,16 @@ int gs3d_set_tuning(gs3d_ctx* c, const gs3d_tuning* t) {
     return fail(c, GS3D_ERR_INVALID_ARG,
                 "raster_batch must be 0 or a multiple of 32 up to 1024 (got %u)",
                 t->raster_batch);
-  if (t->tile_w == 0 || t->tile_h == 0 || t->tile_w * t->tile_h > 1024)
-    return fail(c, GS3D_ERR_INVALID_ARG, "tile %ux%u: 1..1024 pixels", t->tile_w, t->tile_h);
-  TRY(gs3d_set_tile_size(c, t->tile_w, t->tile_h, nullptr, nullptr));
+  // up to 1024 pixels; up to 2048 where the two-pixel raster shades the tile
+  // as row strips of at most 512 threads (sides multiples of 8 and 16)
+  const uint64_t area = (uint64_t)t->tile_w * t->tile_h;
+  const bool wide = area > 1024 && area <= 2048 && t->tile_w % 8 == 0 && t->tile_h % 16 == 0;
+  if (t->tile_w == 0 || t->tile_h == 0 || (area > 1024 && !wide))
+    return fail(c, GS3D_ERR_INVALID_ARG,
+                "tile %ux%u: 1..1024 pixels, or up to 2048 with a width that divides by 8 "
+                "and a height by 16",
+                t->tile_w, t->tile_h);
+  apply_tile_size(c, t->tile_w, t->tile_h);
   c->digit_bits = t->digit_bits;
   c->raster_batch = t->raster_batch;
   return GS3D_OK;
@@ -1216,11 +1237,13 @@ int gs3d_autotune(gs3d_ctx* c, const gs3d_view* views, uint32_t n_views, uint32_
   }
   std::vector<gs3d_tune_result> res;
   int rc = GS3D_OK;
-  const uint32_t tiles[] = {8, 16, 32}, digits[] = {4, 8, 11}, batches[] = {128, 256, 512};
-  for (uint32_t tile : tiles) {
+  // square tiles of 8, 16 and 32, and the 2048-pixel 32x64 and 64x32
+  const uint32_t shapes[][2] = {{8, 8}, {16, 16}, {32, 32}, {32, 64}, {64, 32}};
+  const uint32_t digits[] = {4, 8, 11}, batches[] = {128, 256, 512};
+  for (const auto& shape : shapes) {
     for (uint32_t digit : digits) {
       for (uint32_t batch : batches) {
-        const gs3d_tuning t{tile, tile, digit, batch};
+        const gs3d_tuning t{shape[0], shape[1], digit, batch};
         rc = gs3d_set_tuning(c, &t);
         if (rc != GS3D_OK) break;
         // warm-up: sizes the key buffers (capacity retries), captures the graph

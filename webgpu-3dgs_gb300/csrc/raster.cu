@@ -652,6 +652,9 @@ cudaError_t raster_config(const RasterArgs& a, RasterConfig* cfg) {
   uint32_t split = 1;
   if (mode == 2 && nt > 512) split = (a.tile_h / 4) % 8 == 0 ? 4u : (a.tile_h / 2) % 8 == 0 ? 2u : 1u;
   const uint32_t threads = mode == 2 ? nt / (2 * split) : nt;
+  // one thread a pixel up to 1024 pixels; two-pixel strips of at most 512
+  // threads (the kernel's launch bound)
+  if ((mode != 2 && nt > 1024) || (mode == 2 && threads > 512)) return cudaErrorInvalidValue;
   const size_t smem = 2 * (size_t)D * sizeof(SplatStage);
   auto kern = mode == 2 ? raster_kernel_culled2 : mode == 1 ? raster_kernel_culled
                                                              : raster_kernel_plain;

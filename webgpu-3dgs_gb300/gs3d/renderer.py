@@ -196,12 +196,18 @@ class GaussianSplatRenderer:
     def setTuning(self, tile: int | tuple[int, int] = 16, digit_bits: int = 8,
                   raster_batch: int = 0) -> None:
         """Speed knobs that leave every image bit-identical: square (or
-        (w, h)) tile size, widest tile-id radix digit (4, 6, 8 or 11 bits), splats
-        staged per raster batch (0 = one per tile pixel)."""
+        (w, h)) tile size (up to 1024 pixels, or 2048 with a width that divides
+        by 8 and a height by 16), widest tile-id radix digit (4, 6, 8 or 11
+        bits), splats staged per raster batch (0 = one per tile pixel, at most
+        1024)."""
         tw, th = (tile, tile) if isinstance(tile, int) else tile
         t = _lib.Tuning_t(int(tw), int(th), int(digit_bits), int(raster_batch))
         self._call("gs3d_set_tuning", C.byref(t))
-        self.setTileSize(tw, th)
+        # the tuning may hold tiles above setTileSize's 1024-pixel clamp
+        if (int(tw), int(th)) != (self.tileSizeX, self.tileSizeY):
+            self.lastViewport = (-1, -1)
+        self.tileSizeX, self.tileSizeY = int(tw), int(th)
+        self.scene.tiles = [int(tw), int(th)]
 
     def getTuning(self) -> dict:
         t = _lib.Tuning_t()
