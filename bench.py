@@ -200,12 +200,12 @@ def algorithmic_bytes(n, R, tiles, tile_passes, sh_floats, fused, views_per_scen
 
 # DRAM bytes per unit of the HBM-bound kernels, from ncu captures of a
 # 2-view batch of the same workload (profiles/), scaled to a launch by the
-# units it processes: tile-digit pass per ref (32x32 / 16x16 tiles);
-# preprocess per scene splat read + per splat-view written; emit per
-# (splat-view, ref) at 32x32 tiles with one-word rectangles.
-DRAM_PER_REF_PASS = {32: 22.4, 16: 25.1}
+# units it processes: tile-digit pass per ref (by tile size); preprocess per
+# scene splat read + per splat-view written; emit per (splat-view, ref) with
+# one-word rectangles.
+DRAM_PER_REF_PASS = {(32, 32): 22.4, (16, 16): 25.1, (64, 32): 21.2}
 DRAM_PREPROCESS = (732.1e6 / 3e6, 434.7e6 / 6e6)
-DRAM_EMIT = {32: (365.2e6, 6e6, 23.7e6)}
+DRAM_EMIT = {(32, 32): (365.2e6, 6e6, 23.7e6), (64, 32): (273.4e6, 6e6, 16.99e6)}
 
 
 def dominant_traffic(stage, tile, refs_per_launch, splats_per_launch, scene_splats):
@@ -553,7 +553,8 @@ def run_ours(args, rank, world):
         "tuning": {"tile": [tuned.tile_w, tuned.tile_h], "digit_bits": tuned.digit_bits,
                    "raster_batch": tuned.raster_batch, "candidates": tune_table},
         "tile_passes_batched": tuned_passes,
-        "traffic": dominant_traffic(dom, tuned.tile_w, tuned_R * B, N_SPLATS * B, N_SPLATS),
+        "traffic": dominant_traffic(dom, (tuned.tile_w, tuned.tile_h), tuned_R * B, N_SPLATS * B,
+                                    N_SPLATS),
         "launch_units": {"refs": int(tuned_R * B), "splat_views": N_SPLATS * B},
         "batch_median": batch_median, "c0_gpu_views_per_s": c0_gpu,
         # bytes the sort moves per view: the reference's eight 8-bit passes over
