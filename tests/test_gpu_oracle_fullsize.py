@@ -97,14 +97,18 @@ def test_c1_single_view_16x16_matches_oracle(renderer, oracle, c1, pose):
     assert_frame_match(g, o)
 
 
-def test_c1_headline_batch_32x32_matches_oracle(renderer, oracle, c1):
-    """The bench's first 8-view batch at its autotuned tuning, learned raster
-    order, CUDA-graph replay: views 0 and 5 against the oracle at 32x32."""
+@pytest.mark.parametrize("tw,th,batch,order", [(32, 32, 256, "learned"),
+                                                (64, 32, 512, "key_count")])
+def test_c1_headline_batch_matches_oracle(renderer, oracle, c1, tw, th, batch, order):
+    """The bench's first 8-view batch at an autotuned tuning (64x32 tiles with
+    512-splat batches, the autotuner's pick on this workload, in key-count
+    order; 32x32 with 256-splat batches in the learned order), CUDA-graph
+    replay: views 0 and 5 against the oracle for that tile grid."""
     r = renderer
     r.setSplatData(c1)
-    r.setTuning(32, 8, 256)
-    path = learned.checkpoint_for(32, 32)
-    if path is not None:
+    r.setTuning((tw, th), 8, batch)
+    path = learned.checkpoint_for(tw, th)
+    if order == "learned" and path is not None:
         r.setCostModel(path)
     else:
         r.setSchedule(_lib.SCHEDULE_KEY_COUNT)
@@ -114,7 +118,7 @@ def test_c1_headline_batch_32x32_matches_oracle(renderer, oracle, c1):
         r.rebinBatch(views)  # eager + capture
         r.rebinBatch(views)  # replay
         for v in (0, 5):
-            o = oracle_frame(oracle, c1, views[v][1], W1, H1, 32, 32)
+            o = oracle_frame(oracle, c1, views[v][1], W1, H1, tw, th)
             assert_frame_match(batch_view_frame(r, v), o)
     finally:
         r.setCudaGraph(False)
