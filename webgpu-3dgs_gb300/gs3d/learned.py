@@ -190,7 +190,9 @@ def checkpoint_for(tile_w: int, tile_h: int):
     applies to the tile size it was trained on)."""
     from pathlib import Path
     here = Path(__file__).resolve().parent
-    name = {(16, 16): "cost_mlp_c1.npz", (32, 32): "cost_mlp_c1_t32.npz"}.get((tile_w, tile_h))
+    name = {(16, 16): "cost_mlp_c1.npz", (32, 32): "cost_mlp_c1_t32.npz",
+            (64, 32): "cost_mlp_c1_t64x32.npz",
+            (32, 64): "cost_mlp_c1_t32x64.npz"}.get((tile_w, tile_h))
     return here / name if name and (here / name).exists() else None
 
 
@@ -198,7 +200,7 @@ def main(argv=None) -> None:
     """Trains the cost model of the headline workload (3M-splat cluster
     scene, 1920x1080, 16x16 tiles by default) on random poses at radius
     8-16 and writes the checkpoint:
-    python -m gs3d.learned OUT.npz [--poses 10000] [--heldout 1000] [--tile 16]"""
+    python -m gs3d.learned OUT.npz [--poses 10000] [--heldout 1000] [--tile 16 | WxH]"""
     import argparse
     import time
 
@@ -216,11 +218,12 @@ def main(argv=None) -> None:
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--steps", type=int, default=6000)
     ap.add_argument("--chunk", type=int, default=1000)
-    ap.add_argument("--tile", type=int, default=16)
+    ap.add_argument("--tile", default="16", help="square size or WxH")
     a = ap.parse_args(argv)
     r = GaussianSplatRenderer(Scene())
     r.init()
-    r.setTileSize(a.tile, a.tile)
+    tw, th = (int(v) for v in a.tile.split("x")) if "x" in a.tile else (int(a.tile),) * 2
+    r.setTuning((tw, th), 8, 0)
     # colour does not change a tile's raster cost: SH degree 0 suffices
     r.setSplatData(scenes.scene_clusters(a.splats, seed=0, sh_degree=0))
     total = a.poses + a.heldout
@@ -244,8 +247,8 @@ def main(argv=None) -> None:
     ok = gate(m)
     print(f"collect {t_collect:.1f}s train {t_train:.1f}s held-out {m} gate {'pass' if ok else 'FAIL'}")
     save(a.out, res, m, poses=np.int64(a.poses), heldout=np.int64(a.heldout),
-         workload=np.array(f"{a.splats} splats {a.width}x{a.height} tiles {a.tile}x{a.tile}"),
-         tile=np.int64(a.tile))
+         workload=np.array(f"{a.splats} splats {a.width}x{a.height} tiles {tw}x{th}"),
+         tile=np.array([tw, th], np.int64))
     r.destroy()
 
 
